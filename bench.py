@@ -1,0 +1,423 @@
+#!/usr/bin/env python
+"""ALS epoch benchmark on the 480,189 x 17,770, 100M-rating workload (f = 100, lambda = 0.048).
+
+One step = one ALS epoch (U half-sweep over the CSR, then V half-sweep over the CSC) of the
+library's sweep, inputs resident in HBM.  The timed region is K steps bracketed by a barrier and
+a device synchronize, timed with CUDA events on the stream the library launches on.  The inputs
+(an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors) are far larger than the 129 MB L2, so no
+flush is needed between steps.
+
+The same run also measures, on the same data:
+  * the plain-FP32 sweep (the comparison of the metric), epoch ms and test RMSE after the
+    configured 10 iterations for both precisions;
+  * e2e: the same epoch through the C ABI with HOST buffers: each step re-uploads the ratings
+    from pinned memory (als_reload: H2D, validation, GPU transpose, degree orders), runs the
+    epoch and reads back both factor tables and the test RMSE;
+  * cpu_baseline: the same ALS update on the host cores (the oracle in FP32, OpenMP over rows),
+    timed on a random row sample of each side and scaled to a full epoch.
+
+`--impl reference` times the reference's algorithm on the CPU instead (the reference itself is
+a CUDA program whose removed cuSPARSE call and closed-library dependencies keep it from being
+built here; its restatement in oracle/ is what runs), on the same workload and metric.
+
+Multi-GPU: rows of a half-sweep shard naturally, but every box of this setup has one GPU, so
+`--gpus N` runs N independent replicas (weak scaling); the line reports the slowest replica.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ALS epoch ms & Gram TFLOP/s, batched BF16 vs plain FP32, at equal test RMSE"
+UNIT = "ms/epoch"
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
+    p.add_argument("--scale", type=float, default=1.0)
+    p.add_argument("--precision", choices=["bf16", "fp32", "fp8"], default=None)
+    p.add_argument("--solve", choices=["lu", "cg", "cholesky", "auto"], default="cholesky")
+    p.add_argument("--iters", type=int, default=None, help="iterations for the RMSE comparison")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 comparison")
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    return p.parse_args()
+
+
+def load_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args):
+    import cuda_als_gb300 as ca
+
+    tr, te, info = ca.synth_generate(args.config, scale=args.scale, pinned=True)
+    return tr, te, info
+
+
+def flops_per_half(nnz, rows, f):
+    gram = nnz * f * (f + 1)          # symmetric Gram, unique entries, 2 flops per MAC
+    rhs = 2 * nnz * f
+    solve = rows * (f ** 3 / 3 + 2 * f * f)
+    return gram, rhs, solve
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU legs (the oracle: restated reference algorithm, FP32, OpenMP)
+
+
+def cpu_epoch_estimate(tr, info, seconds, seed=0):
+    """Time the host ALS update on random row samples of both sides; scale to one epoch."""
+    from oracle import oracle as O
+
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    ptr, idx, val = tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, tr.h_csr_coo_vals
+    cptr, cidx, cval = O.csr_to_csc(m, n, ptr, idx, val)
+    U, V = O.init_factors(m, n, f)
+    rng = np.random.default_rng(seed)
+    threads = O.max_threads()
+
+    def timed(frac):
+        su = np.sort(rng.choice(m, size=max(1, int(m * frac)), replace=False)).astype(np.int32)
+        sv = np.sort(rng.choice(n, size=max(1, int(n * frac)), replace=False)).astype(np.int32)
+        t0 = time.perf_counter()
+        O.half_sweep(ptr, idx, val, V, U, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=su)
+        t1 = time.perf_counter()
+        O.half_sweep(cptr, cidx, cval, U, V, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=sv)
+        t2 = time.perf_counter()
+        return (t1 - t0) * m / len(su) + (t2 - t1) * n / len(sv), t2 - t0, len(su), len(sv)
+
+    est, spent, _, _ = timed(0.002)
+    frac = min(1.0, 0.002 * max(1.0, seconds / max(spent, 1e-3)))
+    est, spent, nu, nv = timed(frac)
+    return {"value": est * 1e3, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"random {nu} of {m} rows (U side) and {nv} of {n} rows (V side), "
+                      f"{spent:.1f} s of host time, scaled by rows to one epoch"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    tr, te, info = workload(args)
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    ptr, idx, val = tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, tr.h_csr_coo_vals
+    cptr, cidx, cval = O.csr_to_csc(m, n, ptr, idx, val)
+    U, V = O.init_factors(m, n, f)
+    rng = np.random.default_rng(1)
+    frac = 0.002
+    budget = max(10.0, 150.0 / max(1, args.steps + args.warmup))  # whole run: a few minutes
+
+    def step(frac):
+        su = np.sort(rng.choice(m, size=max(1, int(m * frac)), replace=False)).astype(np.int32)
+        sv = np.sort(rng.choice(n, size=max(1, int(n * frac)), replace=False)).astype(np.int32)
+        t0 = time.perf_counter()
+        O.half_sweep(ptr, idx, val, V, U, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=su)
+        t1 = time.perf_counter()
+        O.half_sweep(cptr, cidx, cval, U, V, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=sv)
+        t2 = time.perf_counter()
+        return ((t1 - t0) * m / len(su) + (t2 - t1) * n / len(sv)) * 1e3, t2 - t0, len(su), len(sv)
+
+    _, spent, _, _ = step(frac)
+    frac = min(1.0, frac * max(1.0, budget / max(spent, 1e-3)))
+    for _ in range(args.warmup):
+        step(frac * 0.25)
+    vals = []
+    for _ in range(args.steps):
+        v, spent, nu, nv = step(frac)
+        vals.append(v)
+    value = float(np.mean(vals))
+    cores = O.max_threads()
+    sample = (f"per step: random {nu} of {m} rows (U side) and {nv} of {n} rows (V side), "
+              f"scaled by rows to one epoch")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, config 3 shapes)",
+        "config": config_dict(args, info, "fp32-host"),
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference's sweep restated on the host (oracle/, FP32, OpenMP over rows, "
+                "per-row Gram + RHS + Cholesky); the reference program itself is CUDA-only",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, info, precision):
+    return {"workload": f"ALS config {args.config}: {info['m']} x {info['n']}, "
+                        f"{info['nnz_train']} train / {info['nnz_test']} test ratings, "
+                        f"f={info['f']}, lambda={info['lambda']:.3f}",
+            "m": info["m"], "n": info["n"], "nnz_train": info["nnz_train"],
+            "nnz_test": info["nnz_test"], "f": info["f"], "precision": precision,
+            "solve": args.solve, "scale": args.scale,
+            "l2": "inputs > L2 (1.8 GB resident vs 129 MB L2): no flush between steps"}
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU leg
+
+
+def run_ours(args):
+    import torch
+
+    import cuda_als_gb300 as ca
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    tr, te, info = workload(args)
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    nnz, nnz_test = info["nnz_train"], info["nnz_test"]
+    iters = args.iters if args.iters is not None else 10
+    solve = {"lu": ca.SOLVE_TYPE.LU, "cg": ca.SOLVE_TYPE.CUMF_ALS_CG_FP32,
+             "cholesky": ca.SOLVE_TYPE.CHOLESKY, "auto": ca.SOLVE_TYPE.AUTO}[args.solve]
+    prec_name = args.precision
+    if prec_name is None:
+        prec_name = "bf16" if f <= 128 and _tc_available(ca) else "fp32"
+    prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16, "fp8": ca.PRECISION.FP8}[prec_name]
+    stream = torch.cuda.Stream()
+
+    def make(precision):
+        mdl = ca.als_model(tr, te, f, lam, iters, ca.CALCULATE_VTVS_TYPE.SMEM_ROW_MAJOR, solve,
+                           32, 1, 1, precision=int(precision), device=local)
+        mdl.set_stream(stream.cuda_stream)
+        return mdl
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def time_epochs(mdl, steps, sampler=None):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        for _ in range(steps):
+            mdl.iterate(1)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        barrier()
+        return e0.elapsed_time(e1) / steps
+
+    def rmse_after(mdl, k):
+        mdl.init_factors()
+        mdl.iterate(k)
+        return mdl.rsme_test()
+
+    peak_hbm, peak_bf16, peak_src = load_peaks()
+
+    # ---- the measured precision
+    model = make(prec)
+    model.init_factors()
+    for _ in range(max(3, args.warmup)):
+        model.iterate(1)
+    with ClockSampler(local) as clk:
+        ms = time_epochs(model, args.steps)
+    clocks = clk.summary()
+    stage = model.stage_ms()
+    counters = model.counters()
+    plan = model.plan(0) if prec != ca.PRECISION.FP32 else None
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    rmse = rmse_after(model, iters)
+
+    # ---- plain FP32 on the same data (the metric's comparison)
+    fp32 = None
+    if not args.no_compare and prec != ca.PRECISION.FP32:
+        ref = make(ca.PRECISION.FP32)
+        ref.init_factors()
+        ref.iterate(2)
+        fms = time_epochs(ref, max(2, min(args.steps, 3)))
+        fstage = ref.stage_ms()
+        frmse = rmse_after(ref, iters)
+        fp32 = {"ms_per_epoch": round(fms, 3), "U_ms": round(fstage["U"], 3),
+                "V_ms": round(fstage["V"], 3), "test_rmse_after_iters": frmse,
+                "speedup": round(fms / ms, 3), "rmse_delta": abs(rmse - frmse)}
+        ref.close()
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        U = np.empty((m, f), np.float32)
+        V = np.empty((n, f), np.float32)
+        model.reload(tr, te)  # warm
+        barrier()
+        t0 = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        for _ in range(args.steps):
+            model.reload(tr, te)
+            model.iterate(1)
+            model.get_factors(U, V)
+            model.rsme_test()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        barrier()
+        wall = (time.perf_counter() - t0) * 1e3 / args.steps
+        ev = e0.elapsed_time(e1) / args.steps
+        h2d = 4 * (m + 1 + 2 * nnz) + 12 * nnz_test
+        d2h = 4 * (m + n) * f + 8
+        e2e = {"value": round(max(ev, wall), 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "device_event_ms": round(ev, 3),
+               "host_wall_ms": round(wall, 3)}
+
+    # ---- roofline of the dominant kernel (the U half-sweep's contraction)
+    gram_u, rhs_u, solve_u = flops_per_half(nnz, m, f)
+    gram_v, rhs_v, solve_v = flops_per_half(nnz, n, f)
+    dom_ms = stage["U"] if stage["U"] >= stage["V"] else stage["V"]
+    dom_side = "U" if stage["U"] >= stage["V"] else "V"
+    dom_flops = gram_u + rhs_u
+    achieved = dom_flops / (dom_ms * 1e-3) / 1e12
+    gram_tflops = (gram_u + gram_v) / (ms * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak_bf16,
+                "unit": "TFLOP/s", "frac": round(achieved / peak_bf16, 4), "traffic": None,
+                "kernel": f"fused half-sweep ({dom_side} side), Gram+RHS flops "
+                          f"nnz*f*(f+1)+2*nnz*f per launch over its CUDA-event time",
+                "peak_source": f"bf16 dense, {peak_src}"}
+    if prec == ca.PRECISION.FP32:
+        roofline["note"] = "FP32 path runs on CUDA cores: the fraction is of the bf16 tensor peak"
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_epoch_estimate(tr, info, args.cpu_seconds)
+
+    launches = int(counters["launches"]) * 2 * args.steps
+    line = {
+        "metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": prec_name, "data": "synthetic (seeded, config 3 shapes; Netflix stand-in)",
+        "config": config_dict(args, info, prec_name),
+        "gram_tflops": round(gram_tflops, 3),
+        "stage_ms": {k: round(v, 3) for k, v in stage.items()},
+        "test_rmse_after_iters": rmse, "iters": iters,
+        "fp32_plain": fp32, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "clocks": clocks, "gpu_launches": launches,
+        "flagged_rows": counters["flagged_rows"],
+    }
+    if plan:
+        line["plan_U"] = plan
+    model.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _tc_available(ca) -> bool:
+    try:
+        cfg = ca.default_config()
+        return True if cfg is not None and os.environ.get("ALS_BENCH_FP32_ONLY") is None else False
+    except Exception:
+        return False
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

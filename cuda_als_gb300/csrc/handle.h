@@ -1,0 +1,62 @@
+// handle.h — the model handle behind als_handle* (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/als_gb300.h"
+
+struct TcState;  // tensor-core path state (sweep_tc.cu)
+
+struct als_handle {
+    als_config cfg{};
+    int precision = ALS_PREC_FP32;  // effective precision
+    int64_t m = 0, n = 0, nnz = 0, nnz_test = 0;
+    int32_t f = 0;
+    cudaStream_t stream = nullptr, own_stream = nullptr;
+
+    // training ratings: CSR (U side) and CSC (V side), row of each CSR entry
+    int32_t *d_csr_ptr = nullptr, *d_csr_idx = nullptr;
+    float *d_csr_val = nullptr;
+    int32_t *d_csc_ptr = nullptr, *d_csc_idx = nullptr;
+    float *d_csc_val = nullptr;
+    int32_t *d_coo_row = nullptr;
+    int32_t *d_csc_perm = nullptr;  // CSC position -> CSR position (built on demand)
+    // test ratings (COO)
+    int32_t *d_test_row = nullptr, *d_test_col = nullptr;
+    float *d_test_val = nullptr;
+    // factors, FP32 row-contiguous (the reference's d_UT / d_VT)
+    float *d_U = nullptr, *d_V = nullptr;
+    // rows of each side in descending-degree order, and the host copy of the pointer arrays
+    int32_t *d_order[2] = {nullptr, nullptr};
+    std::vector<int32_t> host_ptr[2];
+    int32_t maxdeg[2] = {0, 0};
+    // status words and reduction scratch
+    int32_t *d_flags = nullptr;
+    double *d_partials = nullptr, *d_scalar = nullptr;
+
+    void *d_scratch = nullptr;  // transpose / degree-order scratch, allocated once
+    cudaEvent_t ev_transpose[2] = {nullptr, nullptr};
+    std::vector<float> h_U, h_V;  // host mirror written by als_train (h_UT / h_VT)
+    std::string last_error;
+    double stage_ms[4] = {-1.0, -1.0, -1.0, -1.0};
+    int64_t counters[3] = {0, 0, 0};
+    std::vector<cudaEvent_t> events;
+    cudaEvent_t ev_half[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+
+    TcState *tc = nullptr;
+
+    ~als_handle();
+};
+
+// sweep.cpp
+als_status prepare_precision_path(als_handle *h);
+void release_precision_path(als_handle *h);
+void invalidate_graphs(als_handle *h);
+als_status refresh_csc_values(als_handle *h);
+als_status run_half_sweep(als_handle *h, int side, bool timed);
+als_status check_sweep_flags(als_handle *h);
+bool tc_supported(int f);

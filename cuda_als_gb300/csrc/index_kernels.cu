@@ -1,0 +1,400 @@
+// index_kernels.cu — integer work of the sweep, bit-exact: exclusive scan, stable LSD radix sort,
+// stable CSR->CSC transpose and the degree order of rows.
+//
+// The reference transposes offline with scipy (data/netflix/prepare_netflix_data.py:102-109,
+// data/toy_data_2/prepare_toy_data_2.py:195-200: R.tocsr(), R.tocsc()) and loads both layouts
+// from disk (main.cpp:68-71).  Here the CSC is built on the GPU from the CSR: a stable sort of
+// the entries by column index keeps them in row order inside each column, which is exactly the
+// order scipy's csr_tocsc produces.  All of it is HBM-bound integer traffic: coalesced tiles of
+// 4096 keys per CTA, one 256-bin histogram per tile, a device-wide scan of the digit-major
+// histogram matrix, then a stable scatter ranked with warp match-any.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace als {
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 2048
+
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX_BINS = 1 << RADIX_BITS;  // 256 == threads per CTA
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_WARPS = RADIX_THREADS / 32;
+constexpr int RADIX_ROUNDS = 16;                                 // keys per lane
+constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;          // 4096
+constexpr int RADIX_WARP_SPAN = 32 * RADIX_ROUNDS;                // 512 contiguous keys / warp
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Block-wide exclusive scan of per-thread sums (fixed order); returns this thread's prefix and
+// the block total in *total.
+__device__ int block_exclusive_scan(int v, int *total) {
+    __shared__ int warp_sums[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    int warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();  // warp_sums is reused by the next call
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_reduce_kernel(const int32_t *__restrict__ in, int64_t n, int32_t *__restrict__ bsums) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < n) s += in[base + i];
+    int total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) bsums[blockIdx.x] = total;
+}
+
+// One CTA scans the block sums in place (exclusive), looping over tiles with a carry.
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_bsums_kernel(int32_t *__restrict__ bsums, int64_t nb) {
+    int carry = 0;
+    for (int64_t t0 = 0; t0 < nb; t0 += SCAN_TILE) {
+        int64_t base = t0 + (int64_t)threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int s = 0;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            v[i] = base + i < nb ? bsums[base + i] : 0;
+            s += v[i];
+        }
+        int total;
+        int pre = block_exclusive_scan(s, &total) + carry;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            if (base + i < nb) bsums[base + i] = pre;
+            pre += v[i];
+        }
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_apply_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out, int64_t n,
+                  const int32_t *__restrict__ bsums, int with_total) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = base + i < n ? in[base + i] : 0;
+        s += v[i];
+    }
+    int total;
+    int pre = block_exclusive_scan(s, &total) + bsums[blockIdx.x];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) out[base + i] = pre;
+        pre += v[i];
+    }
+    if (with_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_THREADS - 1)
+        out[n] = pre;  // last thread's running sum == grand total
+}
+
+// ---- radix sort -----------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(RADIX_THREADS)
+radix_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int shift, int64_t ntiles,
+                  int32_t *__restrict__ hist) {
+    __shared__ int h[RADIX_BINS];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * RADIX_TILE;
+#pragma unroll 4
+    for (int i = 0; i < RADIX_ROUNDS; ++i) {
+        int64_t pos = base + (int64_t)i * RADIX_THREADS + threadIdx.x;
+        if (pos < n) atomicAdd(&h[(keys[pos] >> shift) & (RADIX_BINS - 1)], 1);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter.  Warp w of tile t owns the contiguous key range [t*4096 + w*512, +512) and
+// walks it in 16 rounds of 32; a key's rank inside its warp is (keys of the same digit in
+// earlier rounds) + (lanes below it with the same digit in this round), found with match.any.
+// The warp offsets per digit are then an exclusive prefix over warps, and the tile offset per
+// digit comes from the scanned digit-major histogram.
+__global__ void __launch_bounds__(RADIX_THREADS)
+radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restrict__ vals_in,
+                     int32_t *__restrict__ keys_out, int32_t *__restrict__ vals_out, int64_t n,
+                     int shift, int64_t ntiles, const int32_t *__restrict__ hist_scan) {
+    __shared__ int wcnt[RADIX_WARPS][RADIX_BINS];
+    __shared__ int goff[RADIX_BINS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int w = 0; w < RADIX_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
+    goff[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+    __syncthreads();
+
+    const int64_t base = (int64_t)blockIdx.x * RADIX_TILE + (int64_t)warp * RADIX_WARP_SPAN;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int32_t key[RADIX_ROUNDS], val[RADIX_ROUNDS];
+    int rank[RADIX_ROUNDS];
+#pragma unroll
+    for (int q = 0; q < RADIX_ROUNDS; ++q) {
+        int64_t pos = base + q * 32 + lane;
+        bool valid = pos < n;
+        key[q] = valid ? keys_in[pos] : 0;
+        val[q] = valid ? (vals_in ? vals_in[pos] : (int32_t)pos) : 0;
+        // invalid lanes get a private digit so they never match a real one
+        int d = valid ? ((key[q] >> shift) & (RADIX_BINS - 1)) : (RADIX_BINS + lane);
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int before = valid ? wcnt[warp][d] : 0;
+        rank[q] = valid ? before + __popc(peers & lt_mask) : -1;
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == lane) wcnt[warp][d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {   // exclusive prefix over warps for digit threadIdx.x
+        int run = 0;
+        for (int w = 0; w < RADIX_WARPS; ++w) {
+            int t = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < RADIX_ROUNDS; ++q) {
+        if (rank[q] < 0) continue;
+        int d = (key[q] >> shift) & (RADIX_BINS - 1);
+        int64_t dst = (int64_t)goff[d] + wcnt[warp][d] + rank[q];
+        keys_out[dst] = key[q];
+        vals_out[dst] = val[q];
+    }
+}
+
+// Row pointers are clamped to [0, nnz]: a malformed pointer array can never write outside.
+__global__ void expand_rows_kernel(int64_t rows, int64_t nnz, const int32_t *__restrict__ ptr,
+                                   int32_t *__restrict__ coo_rows) {
+    const int lane = threadIdx.x & 31;
+    int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = warp; r < rows; r += nwarps) {
+        int32_t b = max(0, min((int32_t)nnz, ptr[r])), e = max(b, min((int32_t)nnz, ptr[r + 1]));
+        for (int32_t k = b + lane; k < e; k += 32) coo_rows[k] = (int32_t)r;
+    }
+}
+
+__global__ void gather_csc_kernel(int64_t nnz, const int32_t *__restrict__ perm,
+                                  const int32_t *__restrict__ coo_rows,
+                                  const float *__restrict__ val, int32_t *__restrict__ ridx,
+                                  float *__restrict__ cval) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        int32_t e = perm[p];
+        ridx[p] = coo_rows[e];
+        cval[p] = val[e];
+    }
+}
+
+// col_ptrs[c] = first position whose sorted key >= c (lower bound), written without atomics.
+__global__ void col_ptrs_from_sorted_kernel(int64_t nnz, int64_t cols,
+                                            const int32_t *__restrict__ skeys,
+                                            int32_t *__restrict__ cptr) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= nnz;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = p == 0 ? 0 : (int64_t)skeys[p - 1] + 1;
+        int64_t hi = p == nnz ? cols : (int64_t)skeys[p];
+        lo = lo < 0 ? 0 : lo;  // keys outside [0, cols) cannot write outside cptr[0..cols]
+        hi = hi > cols ? cols : hi;
+        for (int64_t c = lo; c <= hi; ++c) cptr[c] = (int32_t)p;
+    }
+}
+
+__global__ void degree_keys_kernel(int64_t rows, const int32_t *__restrict__ ptr, int32_t maxd,
+                                   int32_t *__restrict__ keys) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += (int64_t)gridDim.x * blockDim.x)
+        keys[r] = maxd - (ptr[r + 1] - ptr[r]);
+}
+
+__global__ void count_bad_kernel(int64_t nnz, const int32_t *__restrict__ idx, int32_t limit,
+                                 const float *__restrict__ val, int32_t *bad) {
+    int local = 0;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        int32_t c = idx[p];
+        float v = val ? val[p] : 0.0f;
+        if (c < 0 || c >= limit || !isfinite(v)) ++local;
+    }
+    local = __reduce_add_sync(0xffffffffu, local);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(bad, local);
+}
+
+int grid_for(int64_t work, int threads, int cap = 152 * 16) {
+    int64_t g = ceil_div(work > 0 ? work : 1, threads);
+    return (int)(g < cap ? g : cap);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+
+size_t scan_scratch_bytes(int64_t n) {
+    return align256(sizeof(int32_t) * (size_t)(ceil_div(n > 0 ? n : 1, SCAN_TILE) + 1));
+}
+
+cudaError_t exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, bool with_total,
+                               void *scratch, cudaStream_t st) {
+    if (n <= 0) {
+        if (with_total) return cudaMemsetAsync(out, 0, sizeof(int32_t), st);
+        return cudaSuccess;
+    }
+    int64_t nb = ceil_div(n, SCAN_TILE);
+    int32_t *bsums = (int32_t *)scratch;
+    scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, bsums);
+    scan_bsums_kernel<<<1, SCAN_THREADS, 0, st>>>(bsums, nb);
+    scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, out, n, bsums,
+                                                              with_total ? 1 : 0);
+    return cudaGetLastError();
+}
+
+static int radix_passes(int32_t max_key) {
+    int bits = 0;
+    while (bits < 31 && (int64_t(1) << bits) <= (int64_t)max_key) ++bits;
+    int p = (bits + RADIX_BITS - 1) / RADIX_BITS;
+    return p < 1 ? 1 : p;
+}
+
+size_t radix_sort_scratch_bytes(int64_t n) {
+    int64_t ntiles = ceil_div(n > 0 ? n : 1, RADIX_TILE);
+    size_t hist = (size_t)RADIX_BINS * (size_t)ntiles;
+    return 4 * align256(sizeof(int32_t) * (size_t)(n > 0 ? n : 1)) +
+           align256(sizeof(int32_t) * hist) + scan_scratch_bytes((int64_t)hist);
+}
+
+cudaError_t radix_sort_pairs(const int32_t *keys_in, const int32_t *vals_in, int32_t *keys_out,
+                             int32_t *vals_out, int64_t n, int32_t max_key, void *scratch,
+                             cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int64_t ntiles = ceil_div(n, RADIX_TILE);
+    const size_t arr = align256(sizeof(int32_t) * (size_t)n);
+    char *s = (char *)scratch;
+    int32_t *bk[2] = {(int32_t *)s, (int32_t *)(s + 2 * arr)};
+    int32_t *bv[2] = {(int32_t *)(s + arr), (int32_t *)(s + 3 * arr)};
+    s += 4 * arr;
+    int32_t *hist = (int32_t *)s;
+    s += align256(sizeof(int32_t) * (size_t)RADIX_BINS * (size_t)ntiles);
+    void *scan_scratch = s;
+
+    const int passes = radix_passes(max_key);
+    const int32_t *src_k = keys_in, *src_v = vals_in;
+    for (int p = 0; p < passes; ++p) {
+        int32_t *dst_k = p == passes - 1 ? keys_out : bk[p & 1];
+        int32_t *dst_v = p == passes - 1 ? vals_out : bv[p & 1];
+        const int shift = p * RADIX_BITS;
+        radix_hist_kernel<<<(unsigned)ntiles, RADIX_THREADS, 0, st>>>(src_k, n, shift, ntiles,
+                                                                       hist);
+        cudaError_t e = exclusive_scan_i32(hist, hist, (int64_t)RADIX_BINS * ntiles, false,
+                                           scan_scratch, st);
+        if (e != cudaSuccess) return e;
+        radix_scatter_kernel<<<(unsigned)ntiles, RADIX_THREADS, 0, st>>>(
+            src_k, src_v, dst_k, dst_v, n, shift, ntiles, hist);
+        src_k = dst_k;
+        src_v = dst_v;
+    }
+    return cudaGetLastError();
+}
+
+size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz) {
+    (void)rows;
+    (void)cols;
+    const size_t arr = align256(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
+    return 3 * arr + radix_sort_scratch_bytes(nnz);
+}
+
+cudaError_t expand_rows(int64_t rows, int64_t nnz, const int32_t *ptr, int32_t *coo_rows,
+                        cudaStream_t st) {
+    if (rows <= 0) return cudaSuccess;
+    expand_rows_kernel<<<grid_for(rows * 32, 256), 256, 0, st>>>(rows, nnz, ptr, coo_rows);
+    return cudaGetLastError();
+}
+
+cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int32_t *ptr,
+                              const int32_t *idx, const float *val, int32_t *cptr,
+                              int32_t *ridx, float *cval, void *scratch, cudaStream_t st,
+                              int32_t *coo_rows_out, int32_t *perm_out) {
+    if (nnz <= 0) return cudaMemsetAsync(cptr, 0, sizeof(int32_t) * (size_t)(cols + 1), st);
+    const size_t arr = align256(sizeof(int32_t) * (size_t)nnz);
+    char *s = (char *)scratch;
+    int32_t *coo_rows = coo_rows_out ? coo_rows_out : (int32_t *)s;
+    int32_t *skeys = (int32_t *)(s + arr);
+    int32_t *perm = perm_out ? perm_out : (int32_t *)(s + 2 * arr);
+    void *sort_scratch = s + 3 * arr;
+    cudaError_t e = expand_rows(rows, nnz, ptr, coo_rows, st);
+    if (e != cudaSuccess) return e;
+    e = radix_sort_pairs(idx, nullptr, skeys, perm, nnz, (int32_t)(cols > 0 ? cols - 1 : 0),
+                         sort_scratch, st);
+    if (e != cudaSuccess) return e;
+    gather_csc_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, coo_rows, val, ridx, cval);
+    col_ptrs_from_sorted_kernel<<<grid_for(nnz + 1, 256), 256, 0, st>>>(nnz, cols, skeys, cptr);
+    return cudaGetLastError();
+}
+
+size_t degree_order_scratch_bytes(int64_t rows) {
+    return 2 * align256(sizeof(int32_t) * (size_t)(rows > 0 ? rows : 1)) +
+           radix_sort_scratch_bytes(rows);
+}
+
+cudaError_t degree_order_device(int64_t rows, const int32_t *ptr, int32_t max_degree,
+                                int32_t *perm, void *scratch, cudaStream_t st) {
+    if (rows <= 0) return cudaSuccess;
+    const size_t arr = align256(sizeof(int32_t) * (size_t)rows);
+    char *s = (char *)scratch;
+    int32_t *keys = (int32_t *)s;
+    int32_t *skeys = (int32_t *)(s + arr);
+    degree_keys_kernel<<<grid_for(rows, 256), 256, 0, st>>>(rows, ptr, max_degree, keys);
+    return radix_sort_pairs(keys, nullptr, skeys, perm, rows, max_degree, s + 2 * arr, st);
+}
+
+__global__ void gather_f32_kernel(int64_t n, const int32_t *__restrict__ perm,
+                                  const float *__restrict__ src, float *__restrict__ dst) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x)
+        dst[p] = src[perm[p]];
+}
+
+cudaError_t gather_f32(int64_t n, const int32_t *perm, const float *src, float *dst,
+                       cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    gather_f32_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, perm, src, dst);
+    return cudaGetLastError();
+}
+
+cudaError_t count_bad_entries(int64_t nnz, const int32_t *idx, int32_t limit, const float *val,
+                              int32_t *bad, cudaStream_t st) {
+    if (nnz <= 0) return cudaSuccess;
+    count_bad_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, idx, limit, val, bad);
+    return cudaGetLastError();
+}
+
+}  // namespace als

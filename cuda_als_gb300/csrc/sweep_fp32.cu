@@ -1,0 +1,329 @@
+// sweep_fp32.cu — fused FP32 half-sweep: per-row Gram + right-hand side + regularisation + solve
+// in one CTA, nothing but the solution written to HBM.
+//
+// Reference path replaced, per row u of the half-sweep (als_model.cu:1797-2029 for U, :2030-2267
+// for V):
+//   b_u = sum_k r_k y_k             cusparseScsrmm2 + cublasSgeam (als_model.cu:1816-1852)
+//   A_u = sum_k y_k y_k^T + lambda n_u I
+//                                   calculate_vtvs* (als_model.cu:91-167, diag term :157-159)
+//   x_u = A_u^-1 b_u                LU_solve_U/V (getrf no pivot + getrs, :1570-1720)
+//                                   or updateXWithCGHost (cumf_als_cg/cg.cu:683-723)
+// The reference writes every f x f Gram to HBM (d_xtxs) and reads it back in the solver; here
+// the Gram lives in shared memory only.
+//
+// Layout.  The gathered panel Z (KC ratings x FP features, FP32) carries the rating itself as
+// feature f, so the (f+1) x (f+1) Gram of [Y | r] holds A_u in its leading f x f block and b_u in
+// row f.  Each thread owns a 4 x 8 register tile of the lower block triangle (8 x 8 blocks, split
+// in two), so the FMA work is the lower triangle only.  After the last chunk the tiles are
+// stored to shared memory (stride FP+1, conflict-free column walks) and the CTA solves in place.
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "internal.h"
+
+namespace als {
+
+namespace {
+
+constexpr int KC = 32;      // ratings gathered per chunk
+constexpr int MAX_FP = 232; // shared-memory bound of the Gram (FP x (FP+1) floats)
+
+__host__ __device__ inline int fp_of(int f) { return ((f + 1 + 7) / 8) * 8; }
+__host__ __device__ inline int nt_of(int fp) {
+    int nb = fp / 8;
+    int t = nb * (nb + 1);
+    t = (t + 31) / 32 * 32;
+    return t < 64 ? 64 : t;
+}
+__host__ __device__ inline size_t zsize_of(int fp) {
+    size_t z = (size_t)KC * fp, g = (size_t)fp * (fp + 1);
+    return z > g ? z : g;
+}
+inline size_t smem_of(int fp) {
+    return sizeof(float) * (zsize_of(fp) + 2 * KC + 5 * (size_t)fp + 64);
+}
+
+// Deterministic block sum (fixed combination order).
+__device__ float block_sum(float v, float *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < nwarps; ++w) s += red[w];
+        red[32] = s;
+    }
+    __syncthreads();
+    float s = red[32];
+    __syncthreads();
+    return s;
+}
+
+// A(i,j) of the symmetric matrix held as a lower triangle with row stride gs.
+__device__ __forceinline__ float sym(const float *G, int gs, int i, int j) {
+    return i >= j ? G[i * gs + j] : G[j * gs + i];
+}
+
+// ap = A p, one warp per row.
+__device__ void sym_matvec(const float *G, int gs, int f, const float *p, float *ap) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = warp; i < f; i += nwarps) {
+        float s = 0.f;
+        for (int j = lane; j < f; j += 32) s = fmaf(sym(G, gs, i, j), p[j], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) ap[i] = s;
+    }
+    __syncthreads();
+}
+
+// Square-root-free Cholesky A = L D L^T in place on the lower triangle (right-looking; the
+// multipliers l_ik = a_ik / d_k are applied on the fly, so one barrier per column suffices).
+// Returns false, uniformly over the CTA, on a pivot that is not positive and finite.
+__device__ bool ldlt_factor(float *G, int gs, int f) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int k = 0; k < f; ++k) {
+        const float piv = G[k * gs + k];
+        if (!(piv > 0.f) || !isfinite(piv)) return false;
+        const float inv = 1.0f / piv;
+        for (int i = k + 1 + warp; i < f; i += nwarps) {
+            const float lik = G[i * gs + k] * inv;
+            for (int j = k + 1 + lane; j <= i; j += 32) G[i * gs + j] -= lik * G[j * gs + k];
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// x = (L D L^T)^-1 b with warp 0 (b is overwritten).
+__device__ void ldlt_solve(const float *G, int gs, int f, float *b) {
+    if ((threadIdx.x >> 5) == 0) {
+        const int lane = threadIdx.x & 31;
+        for (int k = 0; k < f; ++k) {       // L z = b
+            const float zk = b[k];
+            const float inv = 1.0f / G[k * gs + k];
+            for (int i = k + 1 + lane; i < f; i += 32) b[i] -= G[i * gs + k] * inv * zk;
+            __syncwarp();
+        }
+        for (int k = lane; k < f; k += 32) b[k] = b[k] / G[k * gs + k];  // D w = z
+        __syncwarp();
+        for (int k = f - 1; k >= 0; --k) {  // L^T x = w
+            const float xk = b[k];
+            for (int i = lane; i < k; i += 32) b[i] -= G[k * gs + i] / G[i * gs + i] * xk;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+}
+
+// LU without pivoting of the full matrix (getrf with PivotArray = NULL, als_model.cu:1594),
+// then getrs (:1615-1627).  The lower triangle is mirrored first.
+__device__ bool lu_nopivot_solve(float *G, int gs, int f, float *b) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = warp; i < f; i += nwarps)
+        for (int j = i + 1 + lane; j < f; j += 32) G[i * gs + j] = G[j * gs + i];
+    __syncthreads();
+    for (int k = 0; k < f; ++k) {
+        const float piv = G[k * gs + k];
+        if (piv == 0.f || !isfinite(piv)) return false;
+        const float inv = 1.0f / piv;
+        for (int i = k + 1 + warp; i < f; i += nwarps) {
+            const float l = G[i * gs + k] * inv;
+            for (int j = k + 1 + lane; j < f; j += 32) G[i * gs + j] -= l * G[k * gs + j];
+        }
+        __syncthreads();
+    }
+    if (warp == 0) {
+        for (int k = 0; k < f; ++k) {  // unit-lower L, l_ik = a_ik / u_kk
+            const float zk = b[k];
+            const float inv = 1.0f / G[k * gs + k];
+            for (int i = k + 1 + lane; i < f; i += 32) b[i] -= G[i * gs + k] * inv * zk;
+            __syncwarp();
+        }
+        for (int k = f - 1; k >= 0; --k) {  // upper U
+            __syncwarp();
+            float xk = b[k] / G[k * gs + k];
+            __syncwarp();
+            if (lane == 0) b[k] = xk;
+            for (int i = lane; i < k; i += 32) b[i] -= G[i * gs + k] * xk;
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// Warm-started CG, the algorithm of updateXWithCGKernel (cumf_als_cg/cg.cu:37-232): x from the
+// previous factors, r = b - A x, p = r; per step alpha = r'r / p'Ap, x += alpha p,
+// r -= alpha Ap, exit once r'r < tol, beta = r'r_new / r'r_old, p = r + beta p.  Dot products
+// are summed in a fixed order (the reference uses float atomics).
+__device__ void cg_solve(const float *G, int gs, int f, const float *b, float *x, float *r,
+                         float *p, float *ap, float *red, int iters, float tol) {
+    sym_matvec(G, gs, f, x, ap);
+    float part = 0.f;
+    for (int i = threadIdx.x; i < f; i += blockDim.x) {
+        float ri = b[i] - ap[i];
+        r[i] = ri;
+        p[i] = ri;
+        part += ri * ri;
+    }
+    float rsold = block_sum(part, red);
+    for (int it = 0; it < iters; ++it) {
+        sym_matvec(G, gs, f, p, ap);
+        part = 0.f;
+        for (int i = threadIdx.x; i < f; i += blockDim.x) part += p[i] * ap[i];
+        const float pap = block_sum(part, red);
+        if (!(pap > 0.f)) break;  // exact solution already (r = 0) or breakdown
+        const float alpha = rsold / pap;
+        part = 0.f;
+        for (int i = threadIdx.x; i < f; i += blockDim.x) {
+            x[i] += alpha * p[i];
+            float ri = r[i] - alpha * ap[i];
+            r[i] = ri;
+            part += ri * ri;
+        }
+        const float rsnew = block_sum(part, red);
+        if (rsnew < tol) break;
+        const float beta = rsnew / rsold;
+        rsold = rsnew;
+        for (int i = threadIdx.x; i < f; i += blockDim.x) p[i] = r[i] + beta * p[i];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, const int FP) {
+    extern __shared__ __align__(16) float smem[];
+    const int f = a.f, NB = FP / 8, GS = FP + 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    float *Z = smem;
+    int32_t *scol = (int32_t *)(smem + zsize_of(FP));
+    float *sval = (float *)(scol + KC);
+    float *vb = sval + KC, *vx = vb + FP, *vr = vx + FP, *vp = vr + FP, *vap = vp + FP;
+    float *red = vap + FP;
+
+    const int slot = a.row_begin + blockIdx.x;
+    const int row = a.order ? a.order[slot] : slot;
+    const int beg = a.ptr[row], end = a.ptr[row + 1], nu = end - beg;
+    float *xo = a.X + (int64_t)row * f;
+    if (nu == 0) {  // no ratings: defined as x = 0 (the reference's LU would divide by zero)
+        for (int i = tid; i < f; i += blockDim.x) xo[i] = 0.f;
+        return;
+    }
+
+    // register tile of the lower block triangle
+    const bool active = tid < NB * (NB + 1);
+    const int q = tid >> 1;
+    int bi = (int)((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
+    while ((bi + 1) * (bi + 2) / 2 <= q) ++bi;
+    while (bi * (bi + 1) / 2 > q) --bi;
+    const int bj = q - bi * (bi + 1) / 2;
+    const int r0 = 8 * bi + 4 * (tid & 1), c0 = 8 * bj;
+    float acc[4][8];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[p][c] = 0.f;
+
+    for (int base = beg; base < end; base += KC) {
+        const int cnt = min(KC, end - base);
+        if (tid < KC) {
+            scol[tid] = tid < cnt ? a.idx[base + tid] : -1;
+            sval[tid] = tid < cnt ? a.val[base + tid] : 0.f;
+        }
+        __syncthreads();
+        for (int k = warp; k < KC; k += nwarps) {
+            const int c = scol[k];
+            const float rv = sval[k];
+            const float *y = a.Y + (int64_t)(c < 0 ? 0 : c) * f;
+            for (int j = lane; j < FP; j += 32) {
+                float v = 0.f;
+                if (c >= 0) v = j < f ? __ldg(y + j) : (j == f ? rv : 0.f);
+                Z[k * FP + j] = v;
+            }
+        }
+        __syncthreads();
+        if (active) {
+            for (int k = 0; k < cnt; ++k) {
+                const float4 av = *reinterpret_cast<const float4 *>(&Z[k * FP + r0]);
+                const float4 cv0 = *reinterpret_cast<const float4 *>(&Z[k * FP + c0]);
+                const float4 cv1 = *reinterpret_cast<const float4 *>(&Z[k * FP + c0 + 4]);
+                const float ar[4] = {av.x, av.y, av.z, av.w};
+                const float cr[8] = {cv0.x, cv0.y, cv0.z, cv0.w, cv1.x, cv1.y, cv1.z, cv1.w};
+#pragma unroll
+                for (int p = 0; p < 4; ++p)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) acc[p][c] = fmaf(ar[p], cr[c], acc[p][c]);
+            }
+        }
+        __syncthreads();
+    }
+
+    float *G = Z;  // the Gram of [Y | r] replaces the panel
+    if (active) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) G[(r0 + p) * GS + c0 + c] = acc[p][c];
+    }
+    __syncthreads();
+    const float reg = (float)nu * a.lambda;  // items_cnt * lambda (als_model.cu:157-159)
+    for (int i = tid; i < f; i += blockDim.x) {
+        G[i * GS + i] += reg;
+        vb[i] = G[f * GS + i];
+        vx[i] = xo[i];
+    }
+    __syncthreads();
+
+    bool ok = true;
+    if (a.solve == ALS_SOLVE_CG_FP32 || a.solve == ALS_SOLVE_CG_FP16) {
+        if (a.solve == ALS_SOLVE_CG_FP16) {  // the Gram rounded to binary16 (cg.cu:236-430)
+            for (int i = warp; i < f; i += nwarps)
+                for (int j = lane; j <= i; j += 32)
+                    G[i * GS + j] = __half2float(__float2half_rn(G[i * GS + j]));
+            __syncthreads();
+        }
+        cg_solve(G, GS, f, vb, vx, vr, vp, vap, red, a.cg_iters, a.cg_tol);
+    } else if (a.solve == ALS_SOLVE_LU) {
+        ok = lu_nopivot_solve(G, GS, f, vb);
+        for (int i = tid; i < f; i += blockDim.x) vx[i] = vb[i];
+    } else {
+        ok = ldlt_factor(G, GS, f);
+        if (ok) ldlt_solve(G, GS, f, vb);
+        for (int i = tid; i < f; i += blockDim.x) vx[i] = vb[i];
+    }
+    __syncthreads();
+    float bad = 0.f;
+    for (int i = tid; i < f; i += blockDim.x) bad += isfinite(vx[i]) ? 0.f : 1.f;
+    bad = block_sum(bad, red);
+    if (!ok || bad > 0.f) {
+        for (int i = tid; i < f; i += blockDim.x) xo[i] = 0.f;
+        if (tid == 0 && a.flags) atomicAdd(&a.flags[0], 1);
+        return;
+    }
+    for (int i = tid; i < f; i += blockDim.x) xo[i] = vx[i];
+}
+
+}  // namespace
+
+bool fp32_supported(int f) { return f >= 1 && fp_of(f) <= MAX_FP; }
+
+cudaError_t launch_sweep_fp32(const SweepArgs &a, cudaStream_t st, int *launches) {
+    const int n = a.row_end - a.row_begin;
+    if (n <= 0) return cudaSuccess;
+    const int FP = fp_of(a.f);
+    const size_t smem = smem_of(FP);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(sweep_fp32_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    sweep_fp32_kernel<<<(unsigned)n, nt_of(FP), smem, st>>>(a, FP);
+    if (launches) ++*launches;
+    return cudaGetLastError();
+}
+
+}  // namespace als

@@ -1,0 +1,297 @@
+/*
+ * als_gb300.h — C ABI of the GB300-native ALS (weighted-lambda alternating least squares) sweep.
+ *
+ * Drop-in boundary for vserdyuk/cuda_als.  Every entry point below names the reference interface it
+ * replaces (file:line inside that project).  The ABI is plain C: integers, floats, raw pointers and
+ * sizes.  No C++ types, no torch types, no exceptions cross it; every call returns an als_status.
+ *
+ * Conventions
+ *   - Indices are 0-based int32, values are float32, exactly as the reference's raw .bin arrays
+ *     (cuda_sparse_matrix.h:8-38, cuda_sparse_matrix.cpp:6-27).
+ *   - Factor tables are row-contiguous float32: U[row * f + k], V[col * f + k]
+ *     (the reference's h_UT / h_VT, als_model.h:58-66).
+ *   - A handle owns all of its device memory; views passed to als_create are copied.
+ *   - One handle = one CUDA stream.  A handle is not thread-safe; distinct handles are.
+ *   - Calls are synchronous (they return after the device work finished) unless named *_async.
+ */
+#ifndef ALS_GB300_H
+#define ALS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Replaces the reference's exit(1) inside CUDA_CHECK/CUBLAS_CHECK/CUSPARSE_CHECK
+ * (cuda_common.h:13-91) and std::runtime_error for file/config problems
+ * (cuda_sparse_matrix.cpp:9-27, als_model.cu:1910-1975). */
+typedef enum als_status {
+    ALS_OK = 0,
+    ALS_ERR_INVALID_ARG = 1,  /* bad size, null pointer, index out of range, non-finite rating   */
+    ALS_ERR_IO = 2,           /* missing file, file size not equal to the expected buffer size    */
+    ALS_ERR_CUDA = 3,         /* a CUDA runtime/driver call failed                                */
+    ALS_ERR_NUMERIC = 4,      /* non-positive pivot / non-finite solution flagged by a kernel     */
+    ALS_ERR_TIMEOUT = 5,      /* a bounded device-side wait ran out                               */
+    ALS_ERR_UNSUPPORTED = 6,  /* configuration outside what this build implements                 */
+    ALS_ERR_OUT_OF_MEMORY = 7,
+    ALS_ERR_NO_DEVICE = 8     /* no CUDA device visible                                           */
+} als_status;
+
+/* als_model::CALCULATE_VTVS_TYPE (als_model.h:12-21), same integer values as the INI key
+ * als_calculate_vtvs_type.  Types 0-4 select the FP32 Gram path, 5-7 the BF16 tensor-core path
+ * (tcgen05), unless als_config.precision overrides it.  Type 3 (the reference's load-only
+ * microbenchmark) is accepted and runs the FP32 path. */
+enum {
+    ALS_VTVS_SIMPLE = 0,
+    ALS_VTVS_SMEM_ROW_MAJOR = 1,
+    ALS_VTVS_SMEM_COL_MAJOR = 2,
+    ALS_VTVS_SMEM_ROW_MAJOR_NO_CALC = 3,
+    ALS_VTVS_SMEM_COL_MAJOR_TWO_THREADS = 4,
+    ALS_VTVS_SMEM_ROW_MAJOR_TENSOR = 5,
+    ALS_VTVS_SMEM_ROW_MAJOR_TENSOR_SYMMETRIC = 6,
+    ALS_VTVS_SMEM_ROW_MAJOR_TENSOR_SYMMETRIC_MULT_FRAG = 7
+};
+
+/* als_model::SOLVE_TYPE (als_model.h:23-27), same integer values as the INI key als_solve_type,
+ * plus two solvers of this build. */
+enum {
+    ALS_SOLVE_LU = 0,          /* LU without pivoting (cublasSgetrfBatched with PivotArray=NULL)  */
+    ALS_SOLVE_CG_FP16 = 1,     /* warm-started CG on an FP16-rounded Gram (cg.cu:236-430)          */
+    ALS_SOLVE_CG_FP32 = 2,     /* warm-started CG, FP32 (cg.cu:37-232)                             */
+    ALS_SOLVE_CHOLESKY = 3,    /* batched Cholesky + triangular solves (this build)                */
+    ALS_SOLVE_AUTO = 4         /* per-bucket choice made by the autotuner (this build)             */
+};
+
+/* Arithmetic type of the Gram/RHS contraction. */
+enum {
+    ALS_PREC_FROM_VTVS = -1,   /* derive from calculate_vtvs_type (0-4 -> FP32, 5-7 -> BF16)       */
+    ALS_PREC_FP32 = 0,
+    ALS_PREC_BF16 = 1,
+    ALS_PREC_FP8 = 2           /* e4m3 with a per-row scale                                        */
+};
+
+/* Model configuration.  The first block holds the reference's INI keys and als_model ctor
+ * arguments (main.cpp:28-47, als_model.h:29-32) with the same meaning; the second block holds the
+ * [als_gb300] keys of this build.  Fill with als_config_default() first. */
+typedef struct als_config {
+    int32_t f;                    /* [als] f                                                    */
+    float lambda;                 /* [als] lambda (weighted by the row's rating count)           */
+    int32_t iters;                /* [als] als_iters                                            */
+    int32_t calculate_vtvs_type;  /* [als] als_calculate_vtvs_type                              */
+    int32_t solve_type;           /* [als] als_solve_type                                       */
+    int32_t smem_col_cnt;         /* kept for the ctor signature; hard-coded 32 in main.cpp:43  */
+    int32_t m_batches;            /* [als] m_batches: accepted; rows are bucketed, not batched  */
+    int32_t n_batches;            /* [als] n_batches: accepted; see m_batches                   */
+    /* ---- [als_gb300] ---- */
+    int32_t precision;            /* ALS_PREC_*                                                 */
+    int32_t refine_steps;         /* iterative-refinement steps after a Cholesky solve          */
+    float cond_threshold;         /* diag-ratio estimate above which the residual is FP64       */
+    int32_t cg_steps;             /* CG iterations (reference CG_ITER = 6, als_model.cu:16)     */
+    float cg_tol;                 /* CG exit when r'r < cg_tol (reference CG_ERROR, cg.cu:32)   */
+    int32_t use_graph;            /* capture each half-sweep in a CUDA graph                    */
+    int32_t autotune;             /* time candidate kernels per nnz bucket on the first sweep   */
+    int32_t device;               /* CUDA device ordinal                                        */
+} als_config;
+
+/* Non-owning views of host (or, for *_device entry points, device) arrays.
+ * host_sparse_matrix's CSR / CSC / COO members (cuda_sparse_matrix.h:27-37). */
+typedef struct als_csr_view {
+    int64_t rows, cols, nnz;
+    const int32_t *row_ptrs;   /* rows + 1 */
+    const int32_t *col_idxs;   /* nnz      */
+    const float *vals;         /* nnz      */
+} als_csr_view;
+
+typedef struct als_csc_view {
+    int64_t rows, cols, nnz;
+    const int32_t *col_ptrs;   /* cols + 1 */
+    const int32_t *row_idxs;   /* nnz      */
+    const float *vals;         /* nnz      */
+} als_csc_view;
+
+typedef struct als_coo_view {
+    int64_t rows, cols, nnz;
+    const int32_t *row_idxs;   /* nnz */
+    const int32_t *col_idxs;   /* nnz */
+    const float *vals;         /* nnz */
+} als_coo_view;
+
+typedef struct als_handle als_handle;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Library / configuration                                                                    */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Version string of this build. */
+const char *als_version(void);
+
+/* Human-readable name of a status code. */
+const char *als_status_string(als_status s);
+
+/* Defaults: f=100, lambda=0.05, iters=10, type 1, solve 0 (LU), smem_col_cnt=32, batches 1,
+ * precision from the vtvs type, refine 1, cond 1e4, CG 6 steps / 1e-4, graph on, autotune off. */
+void als_config_default(als_config *cfg);
+
+/* Parse the reference's INI file (keys of main.cpp:28-47 plus an optional [als_gb300] section)
+ * into cfg, and the [data] section into the out-parameters.  data_folder receives at most
+ * data_folder_len bytes (NUL-terminated).  Replaces INIReader usage in main.cpp:21-47. */
+als_status als_config_from_ini(const char *path, als_config *cfg, int64_t *m, int64_t *n,
+                               int64_t *nnz_train, int64_t *nnz_test, int32_t *als_runs,
+                               char *data_folder, size_t data_folder_len);
+
+/* Page-locked host memory for the views (cudaMallocHost / cudaFreeHost), as host_sparse_matrix
+ * holds its arrays (cuda_sparse_matrix.cpp:23, :33-41); H2D copies from it run at full link speed. */
+als_status als_host_alloc(size_t bytes, void **out);
+als_status als_host_free(void *p);
+
+/* Read a raw little-endian .bin array into caller memory; the file size must equal `bytes`.
+ * Replaces host_sparse_matrix::malloc_load_file (cuda_sparse_matrix.cpp:6-27). */
+als_status als_load_bin(const char *path, void *dst, size_t bytes);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Model (als_model, als_model.h:11-80)                                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Construct: copy train CSR (required), train CSC (optional: built on the GPU by a stable
+ * transpose when NULL), test COO (optional) to the device and allocate factors and scratch.
+ * Replaces als_model::als_model (als_model.cu:1517-1552) + device_sparse_matrix ctor
+ * (cuda_sparse_matrix.cpp:76-110).  Views hold HOST pointers. */
+als_status als_create(const als_config *cfg, const als_csr_view *train_csr,
+                      const als_csc_view *train_csc, const als_coo_view *test_coo,
+                      als_handle **out);
+
+/* Same, but the views hold DEVICE pointers (on cfg->device); they are copied device-to-device. */
+als_status als_create_device(const als_config *cfg, const als_csr_view *train_csr,
+                             const als_csc_view *train_csc, const als_coo_view *test_coo,
+                             als_handle **out);
+
+/* Free everything the handle owns.  Replaces als_model::~als_model (als_model.cu:1554-1568). */
+als_status als_destroy(als_handle *h);
+
+/* Last error message recorded on the handle (empty string if none). */
+const char *als_last_error(const als_handle *h);
+
+/* Replace the handle's stream (cudaStream_t passed as void*).  NULL = the handle's own stream. */
+als_status als_set_stream(als_handle *h, void *stream);
+
+/* Upload new ratings of the same sizes (m, n, nnz, nnz_test) into an existing handle, from HOST
+ * views: the CSR (and CSC when given, else the GPU transpose rebuilds it) and the test COO are
+ * copied, validated and re-ordered; the factors are kept.  What a caller with a new rating
+ * snapshot of the same shape does instead of rebuilding als_model (als_model.cu:1517-1552). */
+als_status als_reload(als_handle *h, const als_csr_view *train_csr, const als_csc_view *train_csc,
+                      const als_coo_view *test_coo);
+
+/* Replace the training ratings' VALUES in place (same sparsity pattern), from host memory,
+ * ordered as the CSR given at creation.  The CSC copy is refreshed on the GPU. */
+als_status als_update_values(als_handle *h, const float *csr_vals_host);
+
+/* srand(0); V = 0.2*rand()/RAND_MAX for n*f entries in order; U = 0; upload.
+ * The reference's init (als_model.cu:1772-1784). */
+als_status als_init_factors(als_handle *h);
+
+/* Run `iters` ALS iterations (U half-sweep then V half-sweep each) from the current factors. */
+als_status als_iterate(als_handle *h, int32_t iters);
+
+/* One half-sweep: side 0 solves U given V (rows of the CSR), side 1 solves V given U (CSC).
+ * The U block of als_model::train (als_model.cu:1797-2029) / the V block (:2030-2267). */
+als_status als_half_sweep(als_handle *h, int32_t side);
+
+/* init + cfg.iters iterations + copy factors to the handle's host mirror.
+ * Replaces als_model::train (als_model.cu:1766-2289). */
+als_status als_train(als_handle *h);
+
+/* sqrt(sum((r - u.v)^2) / nnz) over the test / train ratings, accumulated in FP64 in a fixed
+ * order (deterministic).  A factor component that is NaN ends that rating's dot product, as
+ * calculate_square_error does (als_model.cu:62-89).  Replaces rsme_test / rsme_train
+ * (als_model.cu:1722-1764; the reference's spelling "rsme" is kept by the host wrappers). */
+als_status als_rmse_test(als_handle *h, double *out);
+als_status als_rmse_train(als_handle *h, double *out);
+
+/* Copy the factor tables out to / in from host memory (m*f and n*f floats; either may be NULL).
+ * Replaces the public h_UT/h_VT/d_UT/d_VT members (als_model.h:58-66). */
+als_status als_get_factors(als_handle *h, float *U, float *V);
+als_status als_set_factors(als_handle *h, const float *U, const float *V);
+
+/* Raw device pointers of the factor tables (for zero-copy callers). */
+als_status als_get_device_factors(als_handle *h, float **U, float **V);
+
+/* Write the cumf_sgd/libmf binary model: int loss=0, m, n, f, float mean rating, U, V.
+ * Replaces als_model::save_libmf (als_model.cu:2294-2312). */
+als_status als_save_libmf(als_handle *h, const char *path);
+
+/* Shape of the handle: m, n, f, nnz_train, nnz_test (any pointer may be NULL). */
+als_status als_get_shape(const als_handle *h, int64_t *m, int64_t *n, int32_t *f,
+                         int64_t *nnz_train, int64_t *nnz_test);
+
+/* Timing of the last half-sweeps measured with CUDA events on the handle's stream:
+ * out[0] = U half-sweep ms, out[1] = V half-sweep ms, out[2] = quantise ms (BF16/FP8),
+ * out[3] = transpose ms at creation.  Any entry not measured is negative. */
+als_status als_get_stage_ms(const als_handle *h, double out[4]);
+
+/* Counters of the last half-sweep: out[0] = kernel launches, out[1] = rows with a
+ * non-positive pivot or non-finite solution (solved as x = 0 and flagged), out[2] = rows whose
+ * residual was refined in FP64.  */
+als_status als_get_counters(const als_handle *h, int64_t out[3]);
+
+/* The kernel choice per nnz bucket after autotuning: for bucket b, kind[b] (0 = FP32 SIMT,
+ * 1 = BF16 tcgen05, 2 = FP8 tcgen05) and solver[b] (ALS_SOLVE_*).  nb in: capacity, out: count. */
+als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t *kind,
+                        int32_t *solver, int32_t *nb);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Adjoint of the user half-sweep (no reference counterpart; required by the build's spec)     */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Held-out loss L = sum over (u,i,r) in heldout of (r - x_u . y_i)^2 where X = argmin of the
+ * user half-sweep given Y = V.  Computes X (written to the handle's U), L, dL/dY (n*f floats,
+ * host) and dL/dlambda by solving A_u g_u = dL/dx_u with each row's Cholesky factor.
+ * `heldout` is a host COO view (rows index U, cols index V). */
+als_status als_user_halfsweep_adjoint(als_handle *h, const als_coo_view *heldout, double *loss,
+                                      float *dLdY, double *dLdlambda);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Index kernels                                                                              */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Stable CSR -> CSC transpose (rows inside each column ascending, i.e. the order scipy's
+ * tocsc() produces).  The reference does this offline in scipy
+ * (data/netflix/prepare_netflix_data.py:102-109, data/toy_data_2/prepare_toy_data_2.py:195-200).
+ * HOST pointers; output arrays must hold cols+1 / nnz / nnz elements. */
+als_status als_csr_to_csc(const als_csr_view *csr, int32_t *col_ptrs, int32_t *row_idxs,
+                          float *vals);
+
+/* Same, DEVICE pointers, enqueued on `stream` (cudaStream_t as void*); temporary memory is
+ * allocated with cudaMallocAsync on that stream and released before return. */
+als_status als_csr_to_csc_device(const als_csr_view *csr, int32_t *col_ptrs, int32_t *row_idxs,
+                                 float *vals, void *stream);
+
+/* Row order used by the persistent sweep: rows sorted by descending rating count, ties by
+ * ascending row id (a stable sort).  Replaces contiguous m_batches/n_batches splitting
+ * (main.cpp:46-47, als_model.cu:1891-1896).  HOST pointers: row_ptrs (rows+1) in, perm (rows)
+ * out. */
+als_status als_degree_order(int64_t rows, const int32_t *row_ptrs, int32_t *perm);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Synthetic ratings (seeded, deterministic across machines and thread counts)                */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Shapes of the five workload configurations (1..5); see als_synth_generate. */
+als_status als_synth_shape(int32_t config, int64_t *m, int64_t *n, int64_t *nnz_total,
+                           int32_t *f, float *lambda);
+
+/* Generate workload `config` with `seed` at `scale` (1.0 = full size; smaller values shrink
+ * rows, cols and nnz for tests).  Two calls: with NULL arrays to get sizes, then with arrays.
+ * Train is CSR sorted by (row, col); test is COO sorted by (row, col).  Every row and column
+ * keeps at least one training rating. */
+als_status als_synth_generate(int32_t config, uint64_t seed, double scale, int64_t *m, int64_t *n,
+                              int64_t *nnz_train, int64_t *nnz_test, int32_t *row_ptrs,
+                              int32_t *col_idxs, float *vals, int32_t *test_rows,
+                              int32_t *test_cols, float *test_vals);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ALS_GB300_H */
