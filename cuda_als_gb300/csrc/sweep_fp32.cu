@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "internal.h"
+#include "solvers.cuh"
 
 namespace als {
 
@@ -42,156 +43,6 @@ __host__ __device__ inline size_t zsize_of(int fp) {
 }
 inline size_t smem_of(int fp) {
     return sizeof(float) * (zsize_of(fp) + 2 * KC + 5 * (size_t)fp + 64);
-}
-
-// Deterministic block sum (fixed combination order).
-__device__ float block_sum(float v, float *red) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float s = 0.f;
-        for (int w = 0; w < nwarps; ++w) s += red[w];
-        red[32] = s;
-    }
-    __syncthreads();
-    float s = red[32];
-    __syncthreads();
-    return s;
-}
-
-// A(i,j) of the symmetric matrix held as a lower triangle with row stride gs.
-__device__ __forceinline__ float sym(const float *G, int gs, int i, int j) {
-    return i >= j ? G[i * gs + j] : G[j * gs + i];
-}
-
-// ap = A p, one warp per row.
-__device__ void sym_matvec(const float *G, int gs, int f, const float *p, float *ap) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int i = warp; i < f; i += nwarps) {
-        float s = 0.f;
-        for (int j = lane; j < f; j += 32) s = fmaf(sym(G, gs, i, j), p[j], s);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) ap[i] = s;
-    }
-    __syncthreads();
-}
-
-// Square-root-free Cholesky A = L D L^T in place on the lower triangle (right-looking; the
-// multipliers l_ik = a_ik / d_k are applied on the fly, so one barrier per column suffices).
-// Returns false, uniformly over the CTA, on a pivot that is not positive and finite.
-__device__ bool ldlt_factor(float *G, int gs, int f) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int k = 0; k < f; ++k) {
-        const float piv = G[k * gs + k];
-        if (!(piv > 0.f) || !isfinite(piv)) return false;
-        const float inv = 1.0f / piv;
-        for (int i = k + 1 + warp; i < f; i += nwarps) {
-            const float lik = G[i * gs + k] * inv;
-            for (int j = k + 1 + lane; j <= i; j += 32) G[i * gs + j] -= lik * G[j * gs + k];
-        }
-        __syncthreads();
-    }
-    return true;
-}
-
-// x = (L D L^T)^-1 b with warp 0 (b is overwritten).
-__device__ void ldlt_solve(const float *G, int gs, int f, float *b) {
-    if ((threadIdx.x >> 5) == 0) {
-        const int lane = threadIdx.x & 31;
-        for (int k = 0; k < f; ++k) {       // L z = b
-            const float zk = b[k];
-            const float inv = 1.0f / G[k * gs + k];
-            for (int i = k + 1 + lane; i < f; i += 32) b[i] -= G[i * gs + k] * inv * zk;
-            __syncwarp();
-        }
-        for (int k = lane; k < f; k += 32) b[k] = b[k] / G[k * gs + k];  // D w = z
-        __syncwarp();
-        for (int k = f - 1; k >= 0; --k) {  // L^T x = w
-            const float xk = b[k];
-            for (int i = lane; i < k; i += 32) b[i] -= G[k * gs + i] / G[i * gs + i] * xk;
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-}
-
-// LU without pivoting of the full matrix (getrf with PivotArray = NULL, als_model.cu:1594),
-// then getrs (:1615-1627).  The lower triangle is mirrored first.
-__device__ bool lu_nopivot_solve(float *G, int gs, int f, float *b) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int i = warp; i < f; i += nwarps)
-        for (int j = i + 1 + lane; j < f; j += 32) G[i * gs + j] = G[j * gs + i];
-    __syncthreads();
-    for (int k = 0; k < f; ++k) {
-        const float piv = G[k * gs + k];
-        if (piv == 0.f || !isfinite(piv)) return false;
-        const float inv = 1.0f / piv;
-        for (int i = k + 1 + warp; i < f; i += nwarps) {
-            const float l = G[i * gs + k] * inv;
-            for (int j = k + 1 + lane; j < f; j += 32) G[i * gs + j] -= l * G[k * gs + j];
-        }
-        __syncthreads();
-    }
-    if (warp == 0) {
-        for (int k = 0; k < f; ++k) {  // unit-lower L, l_ik = a_ik / u_kk
-            const float zk = b[k];
-            const float inv = 1.0f / G[k * gs + k];
-            for (int i = k + 1 + lane; i < f; i += 32) b[i] -= G[i * gs + k] * inv * zk;
-            __syncwarp();
-        }
-        for (int k = f - 1; k >= 0; --k) {  // upper U
-            __syncwarp();
-            float xk = b[k] / G[k * gs + k];
-            __syncwarp();
-            if (lane == 0) b[k] = xk;
-            for (int i = lane; i < k; i += 32) b[i] -= G[i * gs + k] * xk;
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-    return true;
-}
-
-// Warm-started CG, the algorithm of updateXWithCGKernel (cumf_als_cg/cg.cu:37-232): x from the
-// previous factors, r = b - A x, p = r; per step alpha = r'r / p'Ap, x += alpha p,
-// r -= alpha Ap, exit once r'r < tol, beta = r'r_new / r'r_old, p = r + beta p.  Dot products
-// are summed in a fixed order (the reference uses float atomics).
-__device__ void cg_solve(const float *G, int gs, int f, const float *b, float *x, float *r,
-                         float *p, float *ap, float *red, int iters, float tol) {
-    sym_matvec(G, gs, f, x, ap);
-    float part = 0.f;
-    for (int i = threadIdx.x; i < f; i += blockDim.x) {
-        float ri = b[i] - ap[i];
-        r[i] = ri;
-        p[i] = ri;
-        part += ri * ri;
-    }
-    float rsold = block_sum(part, red);
-    for (int it = 0; it < iters; ++it) {
-        sym_matvec(G, gs, f, p, ap);
-        part = 0.f;
-        for (int i = threadIdx.x; i < f; i += blockDim.x) part += p[i] * ap[i];
-        const float pap = block_sum(part, red);
-        if (!(pap > 0.f)) break;  // exact solution already (r = 0) or breakdown
-        const float alpha = rsold / pap;
-        part = 0.f;
-        for (int i = threadIdx.x; i < f; i += blockDim.x) {
-            x[i] += alpha * p[i];
-            float ri = r[i] - alpha * ap[i];
-            r[i] = ri;
-            part += ri * ri;
-        }
-        const float rsnew = block_sum(part, red);
-        if (rsnew < tol) break;
-        const float beta = rsnew / rsold;
-        rsold = rsnew;
-        for (int i = threadIdx.x; i < f; i += blockDim.x) p[i] = r[i] + beta * p[i];
-        __syncthreads();
-    }
 }
 
 __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, const int FP) {
@@ -278,6 +129,7 @@ __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, con
     __syncthreads();
 
     bool ok = true;
+    const int nt = blockDim.x;
     if (a.solve == ALS_SOLVE_CG_FP32 || a.solve == ALS_SOLVE_CG_FP16) {
         if (a.solve == ALS_SOLVE_CG_FP16) {  // the Gram rounded to binary16 (cg.cu:236-430)
             for (int i = warp; i < f; i += nwarps)
@@ -285,19 +137,19 @@ __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, con
                     G[i * GS + j] = __half2float(__float2half_rn(G[i * GS + j]));
             __syncthreads();
         }
-        cg_solve(G, GS, f, vb, vx, vr, vp, vap, red, a.cg_iters, a.cg_tol);
+        cg_solve<CtaSync>(G, GS, f, vb, vx, vr, vp, vap, red, a.cg_iters, a.cg_tol, tid, nt);
     } else if (a.solve == ALS_SOLVE_LU) {
-        ok = lu_nopivot_solve(G, GS, f, vb);
+        ok = lu_nopivot_solve<CtaSync>(G, GS, f, vb, tid, nt);
         for (int i = tid; i < f; i += blockDim.x) vx[i] = vb[i];
     } else {
-        ok = ldlt_factor(G, GS, f);
-        if (ok) ldlt_solve(G, GS, f, vb);
+        ok = ldlt_factor<CtaSync>(G, GS, f, tid, nt);
+        if (ok) ldlt_solve<CtaSync>(G, GS, f, vb, tid);
         for (int i = tid; i < f; i += blockDim.x) vx[i] = vb[i];
     }
     __syncthreads();
     float bad = 0.f;
     for (int i = tid; i < f; i += blockDim.x) bad += isfinite(vx[i]) ? 0.f : 1.f;
-    bad = block_sum(bad, red);
+    bad = group_sum<CtaSync>(bad, red, tid, nt);
     if (!ok || bad > 0.f) {
         for (int i = tid; i < f; i += blockDim.x) xo[i] = 0.f;
         if (tid == 0 && a.flags) atomicAdd(&a.flags[0], 1);

@@ -1,11 +1,633 @@
-// sweep_tc.cu — tensor-core half-sweep (placeholder until the tcgen05 kernel lands).
+// sweep_tc.cu — tensor-core half-sweep: per-row Gram + right-hand side on tcgen05 (BF16 in, FP32
+// accumulate in TMEM), regularisation and solve fused behind it, nothing but x_u written to HBM.
+//
+// Reference path replaced (per half-sweep, als_model.cu:1797-2029 / :2030-2267):
+//   float2half_array (als_model.cu:54-60)            -> quantise_bf16 below (padded BF16 table)
+//   csrmm2 + geam RHS (als_model.cu:1816-1852)      -> second MMA against the rating tile
+//   calculate_vtvs_smem_row_major_tensor* (:428-1490, wmma 16x16x16, f <= 112 only)
+//                                                    -> tcgen05.mma M=128, N=roundup(f,16)
+//   LU_solve / updateXWithCGHost (:1570-1720, cg.cu) -> solvers.cuh on the Gram in smem
+//
+// One persistent CTA per SM; rows are taken from an atomic counter in descending-degree order, so
+// a 400k-rating row occupies one SM while the others drain the rest.  Warp roles:
+//   warp 0   producer: gathers the factor rows of KC = 64 ratings per stage with 16-byte cp.async
+//            into the 128-byte-swizzled MN-major layout the MMA reads, writes the ratings as row 0
+//            of a K-major tile, and signals the stage (NSTAGE-deep ring of mbarriers).
+//   warp 1   MMA issuer: per 16 ratings one M=128 x N=Ng x K=16 MMA (Gram: A = B = the gathered
+//            panel, both MN-major) and one M=128 x N=16 MMA (RHS: B = the rating tile), into one
+//            of two TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
+//   warps 2-5 epilogue/solver warpgroup: TMEM -> registers -> the FP32 f x f Gram and b in smem,
+//            lambda n_u on the diagonal, then the selected solver; x_u goes to HBM.
+// Operand layout (one stage): 2 atoms of 64 features x KC ratings; atom a, rating k, feature chunk
+// c (8 features, 16 B) sits at a*8192 + (k/8)*1024 + (k%8)*128 + ((c%8) ^ (k%8))*16, i.e. the
+// canonical SWIZZLE_128B MN-major layout with LBO = 8192 (between 64-feature atoms) and
+// SBO = 1024 (between 8-rating groups).  Features f..127 are zero (written once).
+//
+// Every wait is bounded by %globaltimer: a wait that runs out sets the status word, the kernel
+// drains its own MMAs and copies, frees TMEM and returns; the host reports ALS_ERR_TIMEOUT.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "handle.h"
 #include "internal.h"
+#include "solvers.cuh"
 #include "tc.h"
 
-bool tc_path_supported(int f) { (void)f; return false; }
-als_status tc_prepare(als_handle *, std::string *why) { *why = "tensor-core path not built"; return ALS_ERR_UNSUPPORTED; }
-void tc_release(als_handle *) {}
+namespace als {
+namespace tcg {
+
+constexpr int KC = 64;                       // ratings per stage
+constexpr int NSTAGE = 4;
+constexpr int LAG = NSTAGE - 1;              // stages of copies in flight per producer lane
+constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
+constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
+constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
+constexpr int R_BYTES = 2 * ATOM_BYTES;      // K-major rating tile, N = 16 rows x 64 ratings
+constexpr int STAGE_BYTES = TILE_BYTES + R_BYTES;
+constexpr int NTHREADS = 192;                // warp 0 producer, 1 MMA, 2-5 epilogue
+constexpr int EPI_T0 = 64;
+constexpr int EPI_NT = 128;
+constexpr int MAXF = 128;
+constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
+
+struct Meta {  // per stage / per accumulator
+    int32_t row;    // -1 = end of work
+    int32_t cnt;    // ratings in this stage
+    int32_t flags;  // 1 = first stage of the row, 2 = last stage of the row
+    int32_t nu;     // ratings of the row
+};
+
+struct Params {
+    const int32_t *ptr, *idx, *order;
+    const float *val;
+    const __nv_bfloat16 *Ybf;  // (n_opp + 1) x fst, row n_opp all zero
+    float *X;                  // this side's FP32 factors (in: CG warm start, out: solution)
+    int32_t *work;             // atomic row counter (zeroed before the launch)
+    int32_t *flags;            // [0] flagged rows, [1] -, [2] timeouts
+    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, solve, cg_iters;
+    float lambda, cg_tol;
+};
+
+struct Geometry {
+    int fst, ng, acc_cols, acc_stride, tmem_cols, gs;
+    size_t smem;
+};
+
+__host__ __device__ inline int gs_of(int f) { return (f + 1) % 2 ? f + 1 : f + 2; }
+
+inline Geometry geometry(int f) {
+    Geometry g;
+    g.fst = (f + 7) / 8 * 8;
+    g.ng = (f + 15) / 16 * 16;
+    g.acc_cols = g.ng + 16;
+    g.acc_stride = g.acc_cols <= 128 ? 128 : 256;
+    g.tmem_cols = 2 * g.acc_stride;
+    g.gs = gs_of(f);
+    size_t bytes = (size_t)NSTAGE * STAGE_BYTES;                  // operand ring
+    bytes += sizeof(float) * ((size_t)f * g.gs + 5 * 128 + 64);   // Gram, vectors, reduction
+    bytes += sizeof(int32_t) * NSTAGE * KC;                       // gathered column ids
+    bytes += 1024;                                                // metas, barriers, scalars
+    g.smem = bytes + 1024;                                        // 1024-B alignment slack
+    return g;
+}
+
+// ---------------------------------------------------------------------------------- PTX helpers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait; false on timeout or (when abort != nullptr) once another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    for (uint32_t i = 0;; ++i) {
+        if (mbar_try(bar, parity)) return true;
+        if ((i & 255) == 255) {
+            if (abort && *abort) return false;
+            if (now_ns() - t0 > WAIT_NS) return false;
+        }
+    }
+}
+// Warp-uniform wait: lane 0 waits, the outcome is broadcast (no lane can diverge on a timeout).
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort) {
+    int ok = 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor, SWIZZLE_128B, sm_100 layout (version 1 at bits 46-47).
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: D F32, A/B BF16, majors, N, M.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) |
+           ((b_mn ? 1u : 0u) << 16) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ------------------------------------------------------------------------------------- kernels
+
+__global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, int f, int fst,
+                                     __nv_bfloat16 *__restrict__ out) {
+    const int64_t total = rows * (int64_t)fst;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / fst;
+        const int j = (int)(e - r * fst);
+        out[e] = __float2bfloat16_rn(j < f ? Y[r * f + j] : 0.f);
+    }
+}
+
+using EpiSync = NamedSync<1, EPI_NT>;
+
+__global__ void __launch_bounds__(NTHREADS, 1) sweep_tc_kernel(const Params p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int f = p.f, GS = gs_of(f);
+    uint8_t *ring = smem;
+    float *G = (float *)(ring + NSTAGE * STAGE_BYTES);
+    float *vb = G + (size_t)f * GS;
+    float *vx = vb + 128, *vr = vx + 128, *vp = vr + 128, *vap = vp + 128, *red = vap + 128;
+    int32_t *scol = (int32_t *)(red + 64);
+    Meta *smeta = (Meta *)(((uintptr_t)(scol + NSTAGE * KC) + 15) & ~(uintptr_t)15);
+    Meta *ameta = smeta + NSTAGE;
+    uint64_t *bars = (uint64_t *)(ameta + 2);  // 16-byte aligned: Meta is 16 bytes
+    uint64_t *full = bars, *empty = bars + NSTAGE;
+    uint64_t *acc_full = bars + 2 * NSTAGE, *acc_empty = acc_full + 2, *acc_meta = acc_empty + 2;
+    uint64_t *drain = acc_meta + 2;
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    volatile int *abort = (volatile int *)(tmem_slot + 1);
+    volatile int *epi_ok = abort + 1;  // epilogue broadcast of its leader's wait outcome
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
+    for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += NTHREADS)
+        reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&acc_full[b]), 1);
+            mbar_init(smem_u32(&acc_empty[b]), 1);
+            mbar_init(smem_u32(&acc_meta[b]), 1);
+        }
+        mbar_init(smem_u32(drain), 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(p.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------------ producer
+        const int nchunk = p.fst / 8;
+        const char *ybytes = reinterpret_cast<const char *>(p.Ybf);
+        uint32_t it = 0;        // stage counter
+        uint32_t pending = 0;   // stages whose copies are issued but not yet signalled
+        bool ok = true;
+        auto signal_oldest = [&](uint32_t stage_it) {
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[stage_it % NSTAGE]));
+        };
+        while (ok) {
+            int slot = 0;
+            if (lane == 0) slot = atomicAdd(p.work, 1);
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            const bool done = slot >= p.nrows;
+            const int row = done ? -1 : p.order[slot];
+            const int beg = done ? 0 : p.ptr[row], end = done ? 0 : p.ptr[row + 1];
+            const int nu = end - beg;
+            int base = beg;
+            do {  // at least one stage per row (an empty row or the end marker is one stage)
+                const int cnt = done ? 0 : min(KC, end - base);
+                const int s = it % NSTAGE;
+                if (it >= NSTAGE &&
+                    !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t *tile = ring + s * STAGE_BYTES;
+                uint8_t *rt = tile + TILE_BYTES;
+                const int cnt16 = (cnt + 15) & ~15;
+                for (int k = lane; k < KC; k += 32) {
+                    const int c = k < cnt ? p.idx[base + k] : p.zero_row;
+                    scol[s * KC + k] = c;
+                    const float r = k < cnt ? p.val[base + k] : 0.f;
+                    reinterpret_cast<__nv_bfloat16 *>(rt)[k] = __float2bfloat16_rn(r);
+                }
+                __syncwarp();
+                const uint32_t tile_s = smem_u32(tile);
+                for (int e = lane; e < cnt16 * nchunk; e += 32) {
+                    const int k = e / nchunk, c = e - k * nchunk;
+                    const int col = scol[s * KC + k];
+                    const uint32_t dst = tile_s + (c >> 3) * ATOM_STRIDE + (k >> 3) * ATOM_BYTES +
+                                         (k & 7) * 128 + (((c & 7) ^ (k & 7)) << 4);
+                    cp_async16(dst, ybytes + ((size_t)col * p.fst + (size_t)c * 8) * 2);
+                }
+                cp_commit();
+                if (lane == 0) {
+                    Meta m;
+                    m.row = row;
+                    m.cnt = cnt;
+                    m.flags = (base == beg ? 1 : 0) | (done || base + KC >= end ? 2 : 0);
+                    m.nu = nu;
+                    smeta[s] = m;
+                }
+                ++pending;
+                if (pending > LAG) {
+                    cp_wait<LAG>();
+                    signal_oldest(it - LAG);
+                    --pending;
+                }
+                ++it;
+                base += KC;
+            } while (!done && base < end);
+            if (done) break;
+        }
+        cp_wait<0>();
+        while (pending > 0) {  // signal what is still in flight, oldest first
+            signal_oldest(it - pending);
+            --pending;
+        }
+        if (!ok) {
+            *abort = 1;
+            if (lane == 0) atomicAdd(&p.flags[2], 1);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc_g = idesc_bf16(128, p.ng, true, true);
+            const uint32_t idesc_r = idesc_bf16(128, 16, true, false);
+            const uint32_t ring_s = smem_u32(ring);
+            uint32_t it = 0, acc_it = 0, buf = 0;
+            bool ok = true;
+            for (;;) {
+                const int s = it % NSTAGE;
+                if (!mbar_wait(smem_u32(&full[s]), (it / NSTAGE) & 1, abort)) { ok = false; break; }
+                fence_async_smem();
+                tc_fence_after();
+                const Meta m = smeta[s];
+                if (m.row < 0) {  // end of work: tell the epilogue
+                    buf = acc_it & 1;
+                    if (acc_it >= 2 &&
+                        !mbar_wait(smem_u32(&acc_empty[buf]), ((acc_it >> 1) - 1) & 1, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    ameta[buf] = m;
+                    mbar_arrive(smem_u32(&acc_meta[buf]));
+                    break;
+                }
+                if (m.flags & 1) {
+                    buf = acc_it & 1;
+                    if (acc_it >= 2 &&
+                        !mbar_wait(smem_u32(&acc_empty[buf]), ((acc_it >> 1) - 1) & 1, abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                }
+                const uint32_t dg = tmem_base + buf * p.acc_stride;
+                const uint32_t db = dg + p.ng;
+                const uint32_t tile_s = ring_s + s * STAGE_BYTES;
+                const int nk = (m.cnt + 15) >> 4;
+                for (int kk = 0; kk < nk; ++kk) {
+                    const uint64_t ad = sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
+                    const uint64_t rd = sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                    const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
+                    mma_bf16(dg, ad, ad, idesc_g, accum);
+                    mma_bf16(db, ad, rd, idesc_r, accum);
+                }
+                mma_commit(smem_u32(&empty[s]));
+                if (m.flags & 2) {
+                    ameta[buf] = m;
+                    if (m.nu > 0) mma_commit(smem_u32(&acc_full[buf]));
+                    mbar_arrive(smem_u32(&acc_meta[buf]));
+                    ++acc_it;
+                }
+                ++it;
+            }
+            // drain: every MMA issued so far has completed before TMEM is released
+            mma_commit(smem_u32(drain));
+            if (!mbar_wait(smem_u32(drain), 0, nullptr)) ok = false;
+            if (!ok) {
+                *abort = 1;
+                atomicAdd(&p.flags[2], 1);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------------------ epilogue / solver
+        const int et = tid - EPI_T0;                 // 0..127
+        const int lanegrp = (warp & 3) * 32;         // TMEM lanes this warp may read
+        const int i = lanegrp + lane;                // feature row of D held by this thread
+        uint32_t acc_it = 0, fullcnt[2] = {0, 0};
+        bool ok = true;
+        // one leader waits, the warpgroup learns the outcome through shared memory
+        auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
+            if (et == 0) *epi_ok = mbar_wait(bar, parity, abort) ? 1 : 0;
+            EpiSync::sync();
+            const bool r = *epi_ok != 0;
+            EpiSync::sync();
+            return r;
+        };
+        for (;;) {
+            const uint32_t buf = acc_it & 1;
+            if (!group_wait(smem_u32(&acc_meta[buf]), (acc_it >> 1) & 1)) { ok = false; break; }
+            const Meta m = ameta[buf];
+            if (m.row < 0) break;
+            if (m.nu > 0) {
+                if (!group_wait(smem_u32(&acc_full[buf]), fullcnt[buf] & 1)) { ok = false; break; }
+                ++fullcnt[buf];
+                tc_fence_after();
+                const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
+                float v[16];
+                for (int c0 = 0; c0 < p.ng; c0 += 16) {
+                    tmem_ld16(tb + c0, v);
+                    if (i < f) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (c0 + j < f) G[i * GS + c0 + j] = v[j];
+                    }
+                }
+                tmem_ld16(tb + p.ng, v);
+                if (i < f) vb[i] = v[0];
+            }
+            tc_fence_before();
+            EpiSync::sync();
+            if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
+            ++acc_it;
+            float *xo = p.X + (int64_t)m.row * f;
+            if (m.nu == 0) {
+                for (int q = et; q < f; q += EPI_NT) xo[q] = 0.f;
+                continue;
+            }
+            const float reg = (float)m.nu * p.lambda;
+            for (int q = et; q < f; q += EPI_NT) {
+                G[q * GS + q] += reg;
+                vx[q] = xo[q];
+            }
+            EpiSync::sync();
+            bool good = true;
+            if (p.solve == ALS_SOLVE_CG_FP32 || p.solve == ALS_SOLVE_CG_FP16) {
+                cg_solve<EpiSync>(G, GS, f, vb, vx, vr, vp, vap, red, p.cg_iters, p.cg_tol, et,
+                                  EPI_NT);
+            } else if (p.solve == ALS_SOLVE_LU) {
+                good = lu_nopivot_solve<EpiSync>(G, GS, f, vb, et, EPI_NT);
+                for (int q = et; q < f; q += EPI_NT) vx[q] = vb[q];
+            } else {
+                good = ldlt_factor<EpiSync>(G, GS, f, et, EPI_NT);
+                if (good) ldlt_solve<EpiSync>(G, GS, f, vb, et);
+                for (int q = et; q < f; q += EPI_NT) vx[q] = vb[q];
+            }
+            EpiSync::sync();
+            float bad = 0.f;
+            for (int q = et; q < f; q += EPI_NT) bad += isfinite(vx[q]) ? 0.f : 1.f;
+            bad = group_sum<EpiSync>(bad, red, et, EPI_NT);
+            if (!good || bad > 0.f) {
+                for (int q = et; q < f; q += EPI_NT) xo[q] = 0.f;
+                if (et == 0) atomicAdd(&p.flags[0], 1);
+            } else {
+                for (int q = et; q < f; q += EPI_NT) xo[q] = vx[q];
+            }
+            EpiSync::sync();
+        }
+        if (!ok) {
+            *abort = 1;
+            if (et == 0) atomicAdd(&p.flags[2], 1);
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                     "r"(p.tmem_cols)
+                     : "memory");
+}
+
+}  // namespace tcg
+}  // namespace als
+
+// ------------------------------------------------------------------------------------- host side
+
+using namespace als;
+
+struct TcState {
+    tcg::Geometry geo{};
+    __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
+    int32_t *d_work = nullptr;
+    int num_sms = 0;
+    cudaEvent_t ev_q[2] = {nullptr, nullptr};
+};
+
+bool tc_path_supported(int f) { return f >= 1 && f <= tcg::MAXF; }
+
+als_status tc_prepare(als_handle *h, std::string *why) {
+    if (!tc_path_supported(h->f)) {
+        *why = "tensor-core path supports f in 1..128";
+        return ALS_ERR_UNSUPPORTED;
+    }
+    int dev = 0, major = 0, minor = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (major != 10) {
+        *why = "tensor-core path needs a Blackwell (sm_10x) GPU, found sm_" +
+               std::to_string(major) + std::to_string(minor);
+        return ALS_ERR_UNSUPPORTED;
+    }
+    TcState *t = new TcState();
+    h->tc = t;
+    t->geo = tcg::geometry(h->f);
+    t->num_sms = sms;
+    const int64_t opp[2] = {h->n, h->m};  // side 0 gathers V rows, side 1 gathers U rows
+    for (int s = 0; s < 2; ++s) {
+        const size_t bytes = sizeof(__nv_bfloat16) * (size_t)(opp[s] + 1) * t->geo.fst;
+        if (cudaMalloc(&t->d_bf[s], bytes) != cudaSuccess ||
+            cudaMemset(t->d_bf[s], 0, bytes) != cudaSuccess) {
+            *why = "out of memory for the BF16 factor tables";
+            return ALS_ERR_OUT_OF_MEMORY;
+        }
+    }
+    if (cudaMalloc(&t->d_work, sizeof(int32_t) * 4) != cudaSuccess) {
+        *why = "out of memory";
+        return ALS_ERR_OUT_OF_MEMORY;
+    }
+    for (int k = 0; k < 2; ++k) cudaEventCreate(&t->ev_q[k]);
+    cudaError_t e = cudaFuncSetAttribute(tcg::sweep_tc_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)t->geo.smem);
+    if (e != cudaSuccess) {
+        *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        return ALS_ERR_CUDA;
+    }
+    return ALS_OK;
+}
+
+void tc_release(als_handle *h) {
+    TcState *t = h->tc;
+    if (!t) return;
+    for (auto p : t->d_bf)
+        if (p) cudaFree(p);
+    if (t->d_work) cudaFree(t->d_work);
+    for (auto e : t->ev_q)
+        if (e) cudaEventDestroy(e);
+    delete t;
+    h->tc = nullptr;
+}
+
 void tc_invalidate_graphs(als_handle *) {}
+
 als_status tc_values_changed(als_handle *) { return ALS_OK; }
-als_status tc_half_sweep(als_handle *, int, int *, std::string *why) { *why = "tensor-core path not built"; return ALS_ERR_UNSUPPORTED; }
-als_status tc_get_plan(const als_handle *, int, int32_t *, int32_t *, int32_t *, int32_t *nb) { *nb = 0; return ALS_ERR_UNSUPPORTED; }
+
+als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *why) {
+    TcState *t = h->tc;
+    cudaStream_t st = h->stream;
+    const int64_t rows = side == 0 ? h->m : h->n;
+    const int64_t opp = side == 0 ? h->n : h->m;
+    const float *Y = side == 0 ? h->d_V : h->d_U;
+    cudaEventRecord(t->ev_q[0], st);
+    {
+        const int64_t total = opp * t->geo.fst;
+        int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)t->num_sms * 8);
+        tcg::quantise_bf16_kernel<<<grid, 256, 0, st>>>(Y, opp, h->f, t->geo.fst, t->d_bf[side]);
+        ++*launches;
+    }
+    cudaEventRecord(t->ev_q[1], st);
+    cudaMemsetAsync(t->d_work, 0, sizeof(int32_t), st);
+    tcg::Params p{};
+    p.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
+    p.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
+    p.val = side == 0 ? h->d_csr_val : h->d_csc_val;
+    p.order = h->d_order[side];
+    p.Ybf = t->d_bf[side];
+    p.X = side == 0 ? h->d_U : h->d_V;
+    p.work = t->d_work;
+    p.flags = h->d_flags;
+    p.nrows = (int32_t)rows;
+    p.zero_row = (int32_t)opp;
+    p.f = h->f;
+    p.fst = t->geo.fst;
+    p.ng = t->geo.ng;
+    p.acc_stride = t->geo.acc_stride;
+    p.tmem_cols = t->geo.tmem_cols;
+    p.solve = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
+    p.cg_iters = h->cfg.cg_steps;
+    p.lambda = h->cfg.lambda;
+    p.cg_tol = h->cfg.cg_tol;
+    const int grid = (int)std::min<int64_t>(rows, t->num_sms);
+    tcg::sweep_tc_kernel<<<grid, tcg::NTHREADS, t->geo.smem, st>>>(p);
+    ++*launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        *why = std::string("sweep_tc_kernel launch: ") + cudaGetErrorString(e);
+        return ALS_ERR_CUDA;
+    }
+    return ALS_OK;
+}
+
+als_status tc_get_plan(const als_handle *h, int side, int32_t *lo, int32_t *kind,
+                       int32_t *solver, int32_t *nb) {
+    (void)side;
+    if (*nb >= 1) {
+        if (lo) lo[0] = 0;
+        if (kind) kind[0] = h->precision == ALS_PREC_FP8 ? 2 : 1;
+        if (solver) solver[0] = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY
+                                                                    : h->cfg.solve_type;
+    }
+    *nb = 1;
+    return ALS_OK;
+}

@@ -93,17 +93,25 @@ def test_gpu_degree_order_bit_exact(kind):
 
 # ---------------------------------------------------------------- FP32 half-sweeps vs FP64
 
-@pytest.mark.parametrize("f", [1, 10, 20, 64, 100, 128])
-@pytest.mark.parametrize("solve", [ca.SOLVE_TYPE.LU, ca.SOLVE_TYPE.CHOLESKY,
-                                   ca.SOLVE_TYPE.CUMF_ALS_CG_FP32])
-def test_gpu_half_sweep_fp32_matches_oracle(f, solve):
+def _skewed_problem(f):
     rng = np.random.default_rng(100 + f)
     m, n = 400, 300
     degrees = np.minimum(rng.zipf(1.6, m) + 3, n)
     degrees[:3] = [n, n // 2, 1]   # a dense row, a heavy row and a single-rating row
     ptr, idx, val = random_csr(rng, m, n, degrees=degrees)
+    return rng, m, n, ptr, idx, val
+
+
+@pytest.mark.parametrize("f", [1, 10, 20, 64, 100, 128])
+@pytest.mark.parametrize("solve", [ca.SOLVE_TYPE.LU, ca.SOLVE_TYPE.CHOLESKY,
+                                   ca.SOLVE_TYPE.CUMF_ALS_CG_FP32])
+def test_gpu_half_sweep_fp32_matches_oracle(f, solve):
+    """Both half-sweeps from the same inputs.  CG runs its 6 steps without the early exit
+    (cg_tol = 0) so FP32 and FP64 follow the same iteration path."""
+    rng, m, n, ptr, idx, val = _skewed_problem(f)
     lam = 0.05
-    with model_from_csr(m, n, ptr, idx, val, f, lam, solve_type=solve) as mdl:
+    cg_tol = 0.0
+    with model_from_csr(m, n, ptr, idx, val, f, lam, solve_type=solve, cg_tol=cg_tol) as mdl:
         U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
         V0 = (rng.standard_normal((n, f)) * 0.3).astype(np.float32)
         mdl.set_factors(U0, V0)
@@ -115,13 +123,65 @@ def test_gpu_half_sweep_fp32_matches_oracle(f, solve):
         _, V = mdl.get_factors()
     osolve = {0: O.LU, 3: O.CHOLESKY, 2: O.CG_FP32}[int(solve)]
     Ue = U0.copy()
-    O.half_sweep(ptr, idx, val, V0, Ue, f, lam, solve=osolve)
+    O.half_sweep(ptr, idx, val, V0, Ue, f, lam, solve=osolve, cg_tol=cg_tol)
     cptr, ridx, cval = O.csr_to_csc(m, n, ptr, idx, val)
     Ve = V0.copy()
-    O.half_sweep(cptr, ridx, cval, U, Ve, f, lam, solve=osolve)
-    tol = TOL_CG if osolve == O.CG_FP32 else TOL_SOLVE
-    assert rel_rows(U, Ue) < tol
-    assert rel_rows(V, Ve) < tol
+    O.half_sweep(cptr, ridx, cval, U, Ve, f, lam, solve=osolve, cg_tol=cg_tol)
+    if osolve != O.CG_FP32:
+        assert rel_rows(U, Ue) < TOL_SOLVE
+        assert rel_rows(V, Ve) < TOL_SOLVE
+    else:
+        # U-side systems are well conditioned: the FP32 iterates follow FP64's.  On the V side a
+        # 6-step CG that has converged keeps stepping on rounding noise (in FP32 and FP64 alike,
+        # with different noise), so only the residual is comparable there.
+        assert rel_rows(U, Ue) < TOL_CG
+        bn = _rhs_norms(cptr, ridx, cval, U)
+        rg = np.sqrt(_residuals(cptr, ridx, cval, U, V, f, lam) / bn).max()
+        re = np.sqrt(_residuals(cptr, ridx, cval, U, Ve, f, lam) / bn).max()
+        assert rg <= 4 * re + 1e-2
+
+
+def _rhs_norms(ptr, idx, val, Y):
+    out = np.zeros(len(ptr) - 1)
+    for u in range(len(ptr) - 1):
+        cols = idx[ptr[u]:ptr[u + 1]]
+        b = Y[cols].astype(np.float64).T @ val[ptr[u]:ptr[u + 1]]
+        out[u] = b @ b
+    return out
+
+
+def _residuals(ptr, idx, val, Y, X, f, lam):
+    out = np.zeros(len(ptr) - 1)
+    for u in range(len(ptr) - 1):
+        cols = idx[ptr[u]:ptr[u + 1]]
+        Yu = Y[cols].astype(np.float64)
+        A = Yu.T @ Yu + lam * len(cols) * np.eye(f)
+        r = Yu.T @ val[ptr[u]:ptr[u + 1]] - A @ X[u].astype(np.float64)
+        out[u] = r @ r
+    return out
+
+
+@pytest.mark.parametrize("f", [20, 100])
+def test_gpu_cg_exit_rule_matches_reference_semantics(f):
+    """With the reference's exit rule (r'r < 1e-4 after a step, cg.cu:196) a row may stop one
+    step earlier or later in FP32 than in FP64; every GPU row must still end either below the
+    tolerance or after all 6 steps with a residual no worse than 4x the FP64 run's."""
+    rng, m, n, ptr, idx, val = _skewed_problem(f)
+    cptr, ridx, cval = O.csr_to_csc(m, n, ptr, idx, val)
+    U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
+    V0 = (rng.standard_normal((n, f)) * 0.3).astype(np.float32)
+    with model_from_csr(m, n, ptr, idx, val, f, 0.05,
+                        solve_type=ca.SOLVE_TYPE.CUMF_ALS_CG_FP32) as mdl:
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(1)
+        _, V = mdl.get_factors()
+    Ve = V0.copy()
+    O.half_sweep(cptr, ridx, cval, U0, Ve, f, 0.05, solve=O.CG_FP32)
+    rg = _residuals(cptr, ridx, cval, U0, V, f, 0.05)
+    re = _residuals(cptr, ridx, cval, U0, Ve, f, 0.05)
+    assert np.all((rg < 2e-4) | (rg <= 4 * re + 1e-6))
+    close = np.linalg.norm(V - Ve, axis=1) <= 1e-3 * np.maximum(np.linalg.norm(Ve, axis=1), 1e-6)
+    assert close.mean() > 0.9
 
 
 def test_gpu_cg_fp16_mode_runs_close_to_fp32_cg():
