@@ -6,7 +6,8 @@
 //   csrmm2 + geam RHS (als_model.cu:1816-1852)      -> second MMA against the rating tile
 //   calculate_vtvs_smem_row_major_tensor* (:428-1490, wmma 16x16x16, f <= 112 only)
 //                                                    -> tcgen05.mma M=128, N=roundup(f,16)
-//   LU_solve / updateXWithCGHost (:1570-1720, cg.cu) -> solvers.cuh on the Gram in smem
+//   LU_solve / updateXWithCGHost (:1570-1720, cg.cu) -> register solvers (regsolve.cuh) or the
+//                                                       shared-memory LU (solvers.cuh)
 //
 // One persistent CTA per SM; rows are taken from an atomic counter in descending-degree order, so
 // a 400k-rating row occupies one SM while the others drain the rest.  Warp roles:
@@ -15,9 +16,12 @@
 //            of a K-major tile, and signals the stage (NSTAGE-deep ring of mbarriers).
 //   warp 1   MMA issuer: per 16 ratings one M=128 x N=Ng x K=16 MMA (Gram: A = B = the gathered
 //            panel, both MN-major) and one M=128 x N=16 MMA (RHS: B = the rating tile), into one
-//            of two TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
-//   warps 2-5 epilogue/solver warpgroup: TMEM -> registers -> the FP32 f x f Gram and b in smem,
-//            lambda n_u on the diagonal, then the selected solver; x_u goes to HBM.
+//            of NBUF TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
+//   warps 2.. one or two 128-thread solver warpgroups; group g takes every NEPI-th row and owns
+//            two accumulators.  Thread i loads row i of the Gram from TMEM into registers, adds
+//            lambda n_u to its diagonal and runs the selected solver; the accumulator is released
+//            only after refinement, which re-reads A from TMEM for the residual b - A x (in FP64
+//            for rows whose Cholesky diagonal ratio exceeds cond_threshold).
 // Operand layout (one stage): 2 atoms of 64 features x KC ratings; atom a, rating k, feature chunk
 // c (8 features, 16 B) sits at a*8192 + (k/8)*1024 + (k%8)*128 + ((c%8) ^ (k%8))*16, i.e. the
 // canonical SWIZZLE_128B MN-major layout with LBO = 8192 (between 64-feature atoms) and
@@ -33,6 +37,7 @@
 
 #include "handle.h"
 #include "internal.h"
+#include "regsolve.cuh"
 #include "solvers.cuh"
 #include "tc.h"
 
@@ -47,10 +52,8 @@ constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feat
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
 constexpr int R_BYTES = 2 * ATOM_BYTES;      // K-major rating tile, N = 16 rows x 64 ratings
 constexpr int STAGE_BYTES = TILE_BYTES + R_BYTES;
-constexpr int NTHREADS = 192;                // warp 0 producer, 1 MMA, 2-5 epilogue
-constexpr int EPI_T0 = 64;
-constexpr int EPI_NT = 128;
 constexpr int MAXF = 128;
+constexpr int MAX_NBUF = 4;
 constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
 
 struct Meta {  // per stage / per accumulator
@@ -66,31 +69,57 @@ struct Params {
     const __nv_bfloat16 *Ybf;  // (n_opp + 1) x fst, row n_opp all zero
     float *X;                  // this side's FP32 factors (in: CG warm start, out: solution)
     int32_t *work;             // atomic row counter (zeroed before the launch)
-    int32_t *flags;            // [0] flagged rows, [1] -, [2] timeouts
-    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, solve, cg_iters;
-    float lambda, cg_tol;
+    int32_t *flags;            // [0] flagged rows, [1] FP64-refined rows, [2] timeouts
+    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, nepi, solve, cg_iters;
+    int32_t refine_steps;
+    float lambda, cg_tol, cond_threshold;
+};
+
+// Per-warpgroup shared scratch: L rows (or the FP32 Gram for the shared-memory LU), vectors.
+template <int FP>
+struct GroupSmem {
+    static constexpr int LS = FP + 4;
+    static constexpr size_t ls_floats = (size_t)FP * LS;
+    static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
 struct Geometry {
-    int fst, ng, acc_cols, acc_stride, tmem_cols, gs;
+    int fp, fst, ng, acc_stride, tmem_cols, nbuf, nepi, nthreads;
     size_t smem;
 };
 
 __host__ __device__ inline int gs_of(int f) { return (f + 1) % 2 ? f + 1 : f + 2; }
 
+inline int fp_of(int f) {
+    const int r = (f + 15) / 16 * 16;
+    return r <= 32 ? 32 : r <= 64 ? 64 : r <= 112 ? 112 : 128;
+}
+
+inline size_t group_floats(int fp) {
+    switch (fp) {
+    case 32: return GroupSmem<32>::floats;
+    case 64: return GroupSmem<64>::floats;
+    case 112: return GroupSmem<112>::floats;
+    default: return GroupSmem<128>::floats;
+    }
+}
+
 inline Geometry geometry(int f) {
     Geometry g;
+    g.fp = fp_of(f);
     g.fst = (f + 7) / 8 * 8;
     g.ng = (f + 15) / 16 * 16;
-    g.acc_cols = g.ng + 16;
-    g.acc_stride = g.acc_cols <= 128 ? 128 : 256;
-    g.tmem_cols = 2 * g.acc_stride;
-    g.gs = gs_of(f);
-    size_t bytes = (size_t)NSTAGE * STAGE_BYTES;                  // operand ring
-    bytes += sizeof(float) * ((size_t)f * g.gs + 5 * 128 + 64);   // Gram, vectors, reduction
-    bytes += sizeof(int32_t) * NSTAGE * KC;                       // gathered column ids
-    bytes += 1024;                                                // metas, barriers, scalars
-    g.smem = bytes + 1024;                                        // 1024-B alignment slack
+    const int acc_cols = g.ng + 16;
+    g.acc_stride = acc_cols <= 128 ? 128 : 256;
+    g.nbuf = acc_cols <= 128 ? 4 : 2;
+    g.nepi = g.nbuf / 2;
+    g.tmem_cols = g.nbuf * g.acc_stride;
+    g.nthreads = 64 + 128 * g.nepi;
+    size_t bytes = (size_t)NSTAGE * STAGE_BYTES;                     // operand ring
+    bytes += sizeof(float) * group_floats(g.fp) * g.nepi;            // per-group scratch
+    bytes += sizeof(int32_t) * NSTAGE * KC;                          // gathered column ids
+    bytes += 1024;                                                   // metas, barriers, scalars
+    g.smem = bytes + 1024;                                           // 1024-B alignment slack
     return g;
 }
 
@@ -214,38 +243,155 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
     }
 }
 
-using EpiSync = NamedSync<1, EPI_NT>;
+// sum_j D[i][j] x_j re-read from TMEM in 16-column chunks (FP64 products and sums when WIDE)
+template <int FP, bool WIDE>
+__device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *xs) {
+    double acc = 0.0;
+    float accf = 0.f;
+#pragma unroll
+    for (int c = 0; c < FP; c += 16) {
+        if (c < ng) {
+            float v[16];
+            tmem_ld16(tb + c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                if (WIDE)
+                    acc = fma((double)v[j], (double)xs[c + j], acc);
+                else
+                    accf = fmaf(v[j], xs[c + j], accf);
+            }
+        }
+    }
+    return WIDE ? acc : (double)accf;
+}
 
-__global__ void __launch_bounds__(NTHREADS, 1) sweep_tc_kernel(const Params p) {
+// The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
+template <int FP>
+__device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
+                          float *gsm, const GroupSync &gs) {
+    float *Ls = gsm;
+    float *sv = gsm + GroupSmem<FP>::ls_floats;
+    float *yv = sv + FP;
+    float *red = yv + FP;
+    float *vec = red + 16;  // 5 x 128 floats for the shared-memory solvers
+    const int f = p.f;
+    float *xo = p.X + (int64_t)m.row * f;
+    const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
+
+    float a[FP];
+#pragma unroll
+    for (int c = 0; c < FP; c += 16) {
+        if (c < p.ng) {
+            tmem_ld16(tb + c, &a[c]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) a[c + j] = 0.f;
+        }
+    }
+    float bi;
+    {
+        float v[16];
+        tmem_ld16(tb + p.ng, v);
+        bi = i < f ? v[0] : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < FP; ++j)
+        if (j == i) a[j] = i < f ? a[j] + reg : 1.f;  // identity on the padded rows
+
+    int slot = 0;
+    float xi = 0.f;
+    bool good = true;
+    if (p.solve == ALS_SOLVE_CG_FP32 || p.solve == ALS_SOLVE_CG_FP16) {
+        xi = cg_reg<FP>(a, bi, i < f ? xo[i] : 0.f, i, sv, red, p.cg_iters, p.cg_tol, gs);
+    } else if (p.solve == ALS_SOLVE_LU) {
+        // reference semantics: LU without pivoting of the full matrix, in shared memory
+        const int GS = gs_of(f);
+        float *G = Ls;
+        if (i < f) {
+#pragma unroll
+            for (int j = 0; j < FP; ++j)
+                if (j < f) G[i * GS + j] = a[j];
+        }
+        float *vb = vec;
+        if (i < f) vb[i] = bi;
+        gs.sync();
+        if (g == 0)
+            good = lu_nopivot_solve<NamedSync<1, 128>>(G, GS, f, vb, et, 128);
+        else
+            good = lu_nopivot_solve<NamedSync<2, 128>>(G, GS, f, vb, et, 128);
+        xi = i < f ? vb[i] : 0.f;
+        gs.sync();
+    } else {
+        // Cholesky (+ refinement against the TMEM copy of A)
+        good = chol_reg<FP>(a, i, Ls, gs);
+        const float bad = gsum128(good ? 0.f : 1.f, red, slot, gs);
+        good = bad == 0.f;
+        if (good) {
+            xi = chol_solve_reg<FP>(a, bi, i, Ls, yv, gs);
+            // condition estimate from the Cholesky diagonal: (max L_ii / min L_ii)^2
+            float lii = 1.f;
+#pragma unroll
+            for (int j = 0; j < FP; ++j)
+                if (j == i) lii = a[j];
+            const float dmax = gmax128(i < f ? lii : 0.f, red, slot, gs);
+            const float dmin = -gmax128(i < f ? -lii : -3.0e38f, red, slot, gs);
+            const bool wide = (dmax / dmin) * (dmax / dmin) > p.cond_threshold;
+            for (int s = 0; s < p.refine_steps; ++s) {
+                sv[i] = i < f ? xi : 0.f;
+                gs.sync();
+                const double ax = wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
+                                       : tmem_rowdot<FP, false>(tb, p.ng, sv);
+                float ri;
+                if (wide)
+                    ri = (float)((double)bi - ax - (double)reg * (double)xi);
+                else
+                    ri = bi - (float)ax - reg * xi;
+                if (i >= f) ri = 0.f;
+                const float di = chol_solve_reg<FP>(a, ri, i, Ls, yv, gs);
+                xi += di;
+            }
+            if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
+        }
+    }
+    const float nonfinite = gsum128((i < f && !isfinite(xi)) ? 1.f : 0.f, red, slot, gs);
+    if (!good || nonfinite > 0.f) {
+        if (i < f) xo[i] = 0.f;
+        if (et == 0) atomicAdd(&p.flags[0], 1);
+    } else if (i < f) {
+        xo[i] = xi;
+    }
+}
+
+template <int FP>
+__global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const int f = p.f, GS = gs_of(f);
     uint8_t *ring = smem;
-    float *G = (float *)(ring + NSTAGE * STAGE_BYTES);
-    float *vb = G + (size_t)f * GS;
-    float *vx = vb + 128, *vr = vx + 128, *vp = vr + 128, *vap = vp + 128, *red = vap + 128;
-    int32_t *scol = (int32_t *)(red + 64);
+    float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
+    int32_t *scol = (int32_t *)(gscratch + GroupSmem<FP>::floats * p.nepi);
     Meta *smeta = (Meta *)(((uintptr_t)(scol + NSTAGE * KC) + 15) & ~(uintptr_t)15);
     Meta *ameta = smeta + NSTAGE;
-    uint64_t *bars = (uint64_t *)(ameta + 2);  // 16-byte aligned: Meta is 16 bytes
+    uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
     uint64_t *full = bars, *empty = bars + NSTAGE;
-    uint64_t *acc_full = bars + 2 * NSTAGE, *acc_empty = acc_full + 2, *acc_meta = acc_empty + 2;
-    uint64_t *drain = acc_meta + 2;
+    uint64_t *acc_full = bars + 2 * NSTAGE;
+    uint64_t *acc_empty = acc_full + MAX_NBUF, *acc_meta = acc_empty + MAX_NBUF;
+    uint64_t *drain = acc_meta + MAX_NBUF;
     uint32_t *tmem_slot = (uint32_t *)(drain + 1);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
-    volatile int *epi_ok = abort + 1;  // epilogue broadcast of its leader's wait outcome
+    volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nbuf = 2 * p.nepi;
 
     // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
-    for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += NTHREADS)
+    for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += blockDim.x)
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
             mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < MAX_NBUF; ++b) {
             mbar_init(smem_u32(&acc_full[b]), 1);
             mbar_init(smem_u32(&acc_empty[b]), 1);
             mbar_init(smem_u32(&acc_meta[b]), 1);
@@ -351,32 +497,30 @@ __global__ void __launch_bounds__(NTHREADS, 1) sweep_tc_kernel(const Params p) {
             const uint32_t ring_s = smem_u32(ring);
             uint32_t it = 0, acc_it = 0, buf = 0;
             bool ok = true;
+            auto take_buffer = [&]() -> bool {  // wait until accumulator acc_it % nbuf is free
+                buf = acc_it % nbuf;
+                const uint32_t use = acc_it / nbuf;
+                if (use >= 1 && !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort))
+                    return false;
+                tc_fence_after();
+                return true;
+            };
             for (;;) {
                 const int s = it % NSTAGE;
                 if (!mbar_wait(smem_u32(&full[s]), (it / NSTAGE) & 1, abort)) { ok = false; break; }
                 fence_async_smem();
                 tc_fence_after();
                 const Meta m = smeta[s];
-                if (m.row < 0) {  // end of work: tell the epilogue
-                    buf = acc_it & 1;
-                    if (acc_it >= 2 &&
-                        !mbar_wait(smem_u32(&acc_empty[buf]), ((acc_it >> 1) - 1) & 1, abort)) {
-                        ok = false;
-                        break;
+                if (m.row < 0) {  // end of work: one end marker per solver warpgroup
+                    for (int g = 0; g < p.nepi && ok; ++g) {
+                        if (!take_buffer()) { ok = false; break; }
+                        ameta[buf] = m;
+                        mbar_arrive(smem_u32(&acc_meta[buf]));
+                        ++acc_it;
                     }
-                    ameta[buf] = m;
-                    mbar_arrive(smem_u32(&acc_meta[buf]));
                     break;
                 }
-                if (m.flags & 1) {
-                    buf = acc_it & 1;
-                    if (acc_it >= 2 &&
-                        !mbar_wait(smem_u32(&acc_empty[buf]), ((acc_it >> 1) - 1) & 1, abort)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                }
+                if ((m.flags & 1) && !take_buffer()) { ok = false; break; }
                 const uint32_t dg = tmem_base + buf * p.acc_stride;
                 const uint32_t db = dg + p.ng;
                 const uint32_t tile_s = ring_s + s * STAGE_BYTES;
@@ -406,81 +550,43 @@ __global__ void __launch_bounds__(NTHREADS, 1) sweep_tc_kernel(const Params p) {
             }
         }
         __syncwarp();
-    } else {
-        // ------------------------------------------------------------------ epilogue / solver
-        const int et = tid - EPI_T0;                 // 0..127
+    } else if (warp < 2 + 4 * p.nepi) {
+        // ------------------------------------------------------------------ solver warpgroups
+        const int g = (warp - 2) >> 2;
+        const int et = tid - 64 - 128 * g;           // 0..127 inside the group
         const int lanegrp = (warp & 3) * 32;         // TMEM lanes this warp may read
-        const int i = lanegrp + lane;                // feature row of D held by this thread
-        uint32_t acc_it = 0, fullcnt[2] = {0, 0};
+        const int i = lanegrp + lane;                // row of the Gram held by this thread
+        const GroupSync gs{1 + g};
+        float *gsm = gscratch + GroupSmem<FP>::floats * g;
+        volatile int *okflag = grp_ok + g;
+        uint32_t fullcnt[2] = {0, 0};
         bool ok = true;
-        // one leader waits, the warpgroup learns the outcome through shared memory
         auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
-            if (et == 0) *epi_ok = mbar_wait(bar, parity, abort) ? 1 : 0;
-            EpiSync::sync();
-            const bool r = *epi_ok != 0;
-            EpiSync::sync();
+            if (et == 0) *okflag = mbar_wait(bar, parity, abort) ? 1 : 0;
+            gs.sync();
+            const bool r = *okflag != 0;
+            gs.sync();
             return r;
         };
-        for (;;) {
-            const uint32_t buf = acc_it & 1;
-            if (!group_wait(smem_u32(&acc_meta[buf]), (acc_it >> 1) & 1)) { ok = false; break; }
+        for (uint32_t acc_it = g;; acc_it += p.nepi) {
+            const uint32_t buf = acc_it % nbuf;
+            const uint32_t use = acc_it / nbuf;
+            const int lb = (int)(buf / p.nepi);      // 0/1: this group's two buffers
+            if (!group_wait(smem_u32(&acc_meta[buf]), use & 1)) { ok = false; break; }
             const Meta m = ameta[buf];
             if (m.row < 0) break;
             if (m.nu > 0) {
-                if (!group_wait(smem_u32(&acc_full[buf]), fullcnt[buf] & 1)) { ok = false; break; }
-                ++fullcnt[buf];
+                if (!group_wait(smem_u32(&acc_full[buf]), fullcnt[lb] & 1)) { ok = false; break; }
+                ++fullcnt[lb];
                 tc_fence_after();
                 const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
-                float v[16];
-                for (int c0 = 0; c0 < p.ng; c0 += 16) {
-                    tmem_ld16(tb + c0, v);
-                    if (i < f) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            if (c0 + j < f) G[i * GS + c0 + j] = v[j];
-                    }
-                }
-                tmem_ld16(tb + p.ng, v);
-                if (i < f) vb[i] = v[0];
+                solve_row<FP>(p, m, tb, i, et, g, gsm, gs);
+            } else if (i < p.f) {
+                p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
             }
             tc_fence_before();
-            EpiSync::sync();
+            gs.sync();
             if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
-            ++acc_it;
-            float *xo = p.X + (int64_t)m.row * f;
-            if (m.nu == 0) {
-                for (int q = et; q < f; q += EPI_NT) xo[q] = 0.f;
-                continue;
-            }
-            const float reg = (float)m.nu * p.lambda;
-            for (int q = et; q < f; q += EPI_NT) {
-                G[q * GS + q] += reg;
-                vx[q] = xo[q];
-            }
-            EpiSync::sync();
-            bool good = true;
-            if (p.solve == ALS_SOLVE_CG_FP32 || p.solve == ALS_SOLVE_CG_FP16) {
-                cg_solve<EpiSync>(G, GS, f, vb, vx, vr, vp, vap, red, p.cg_iters, p.cg_tol, et,
-                                  EPI_NT);
-            } else if (p.solve == ALS_SOLVE_LU) {
-                good = lu_nopivot_solve<EpiSync>(G, GS, f, vb, et, EPI_NT);
-                for (int q = et; q < f; q += EPI_NT) vx[q] = vb[q];
-            } else {
-                good = ldlt_factor<EpiSync>(G, GS, f, et, EPI_NT);
-                if (good) ldlt_solve<EpiSync>(G, GS, f, vb, et);
-                for (int q = et; q < f; q += EPI_NT) vx[q] = vb[q];
-            }
-            EpiSync::sync();
-            float bad = 0.f;
-            for (int q = et; q < f; q += EPI_NT) bad += isfinite(vx[q]) ? 0.f : 1.f;
-            bad = group_sum<EpiSync>(bad, red, et, EPI_NT);
-            if (!good || bad > 0.f) {
-                for (int q = et; q < f; q += EPI_NT) xo[q] = 0.f;
-                if (et == 0) atomicAdd(&p.flags[0], 1);
-            } else {
-                for (int q = et; q < f; q += EPI_NT) xo[q] = vx[q];
-            }
-            EpiSync::sync();
         }
         if (!ok) {
             *abort = 1;
@@ -495,6 +601,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) sweep_tc_kernel(const Params p) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                      "r"(p.tmem_cols)
                      : "memory");
+}
+
+template <int FP>
+cudaError_t configure(size_t smem) {
+    return cudaFuncSetAttribute(sweep_tc_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
+}
+
+template <int FP>
+void launch(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
+    sweep_tc_kernel<FP><<<grid, g.nthreads, g.smem, st>>>(p);
 }
 
 }  // namespace tcg
@@ -547,9 +664,13 @@ als_status tc_prepare(als_handle *h, std::string *why) {
         return ALS_ERR_OUT_OF_MEMORY;
     }
     for (int k = 0; k < 2; ++k) cudaEventCreate(&t->ev_q[k]);
-    cudaError_t e = cudaFuncSetAttribute(tcg::sweep_tc_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)t->geo.smem);
+    cudaError_t e;
+    switch (t->geo.fp) {
+    case 32: e = tcg::configure<32>(t->geo.smem); break;
+    case 64: e = tcg::configure<64>(t->geo.smem); break;
+    case 112: e = tcg::configure<112>(t->geo.smem); break;
+    default: e = tcg::configure<128>(t->geo.smem); break;
+    }
     if (e != cudaSuccess) {
         *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
         return ALS_ERR_CUDA;
@@ -604,12 +725,20 @@ als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *wh
     p.ng = t->geo.ng;
     p.acc_stride = t->geo.acc_stride;
     p.tmem_cols = t->geo.tmem_cols;
+    p.nepi = t->geo.nepi;
     p.solve = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
     p.cg_iters = h->cfg.cg_steps;
+    p.refine_steps = h->cfg.refine_steps;
     p.lambda = h->cfg.lambda;
     p.cg_tol = h->cfg.cg_tol;
+    p.cond_threshold = h->cfg.cond_threshold;
     const int grid = (int)std::min<int64_t>(rows, t->num_sms);
-    tcg::sweep_tc_kernel<<<grid, tcg::NTHREADS, t->geo.smem, st>>>(p);
+    switch (t->geo.fp) {
+    case 32: tcg::launch<32>(p, t->geo, grid, st); break;
+    case 64: tcg::launch<64>(p, t->geo, grid, st); break;
+    case 112: tcg::launch<112>(p, t->geo, grid, st); break;
+    default: tcg::launch<128>(p, t->geo, grid, st); break;
+    }
     ++*launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

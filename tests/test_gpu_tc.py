@@ -17,7 +17,8 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-TOL_BF16_INPUTS = 2e-4   # GPU vs FP64 oracle on BF16-rounded factors (exact-solve modes)
+TOL_BF16_INPUTS = 5e-4   # GPU vs FP64 oracle on BF16-rounded factors (FP32 accumulation of up
+                         # to thousands of products per Gram entry, exact-solve modes)
 TOL_BF16_RMSE = 2e-3     # test RMSE, BF16 vs plain FP32 after training
 
 
