@@ -1,8 +1,10 @@
 // regsolve.cuh — register-resident per-row solvers for the tensor-core epilogue.
 //
 // After tcgen05.ld, thread i of a 128-thread solver warpgroup holds row i of the (padded) Gram
-// A in registers (a[0..FP)), and b_i.  Rows i >= f are padded with the identity, so every
-// solver runs at the compile-time size FP (a multiple of 16) and leaves x_i = 0 there.
+// A in registers (a[0..FP)), and b_i.  Rows f <= i < FP are padded with the identity, so every
+// solver runs at the compile-time size FP (a multiple of 16) and leaves x_i = 0 there.  Threads
+// with i >= FP (FP < 128) hold zero rows: they join every barrier and shuffle but never index
+// shared memory with i.
 //
 //   cg_reg        warm-started CG of cumf_als_cg/cg.cu:37-232 (same recurrences, same exit rule
 //                 r'r < tol); the matvec reads p from shared memory as float4 broadcasts.
@@ -66,13 +68,14 @@ template <int FP>
 __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *sv, float *red,
                         int iters, float tol, const GroupSync &gs) {
     int slot = 0;
-    sv[i] = xi;
+    const bool live = i < FP;  // threads past the padded size hold zero rows and write nothing
+    if (live) sv[i] = xi;
     gs.sync();
     float r = bi - dot_row<FP>(a, sv);
     float p = r;
     float rsold = gsum128(r * r, red, slot, gs);
     for (int it = 0; it < iters; ++it) {
-        sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
+        if (live) sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
         gs.sync();
         const float ap = dot_row<FP>(a, sv);
         const float pap = gsum128(p * ap, red, slot, gs);
@@ -156,7 +159,7 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, const GroupSync &gs) 
         }
         gs.sync();
         // rows below the block: the 8 x 8 triangular solve against the published block rows
-        if (active && i >= k0 + B) {
+        if (active && i >= k0 + B && i < FP) {
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
                 const float *lk = Ls + (k0 + kk) * LS;
@@ -207,7 +210,7 @@ __device__ float chol_solve_reg(const float (&a)[FP], float bi, int i, const flo
     }
     gs.sync();
     // backward: x_i = (y_i - sum_{j>i} L_ji x_j) / L_ii, blocks from the bottom
-    float x = yv[i];
+    float x = i < FP ? yv[i] : 0.f;
 #pragma unroll
     for (int K = FP / B - 1; K >= 0; --K) {
         const int k0 = K * B;

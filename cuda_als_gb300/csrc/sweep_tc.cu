@@ -337,7 +337,7 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             const float dmin = -gmax128(i < f ? -lii : -3.0e38f, red, slot, gs);
             const bool wide = (dmax / dmin) * (dmax / dmin) > p.cond_threshold;
             for (int s = 0; s < p.refine_steps; ++s) {
-                sv[i] = i < f ? xi : 0.f;
+                if (i < FP) sv[i] = i < f ? xi : 0.f;
                 gs.sync();
                 const double ax = wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
                                        : tmem_rowdot<FP, false>(tb, p.ng, sv);
