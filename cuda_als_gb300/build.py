@@ -25,6 +25,10 @@ SOURCES = [
     "index_kernels.cu",
     "sweep_fp32.cu",
     "sweep_tc.cu",
+    "sweep_tc_fp32.cu",
+    "sweep_tc_fp64.cu",
+    "sweep_tc_fp112.cu",
+    "sweep_tc_fp128.cu",
     "rmse.cu",
     "adjoint.cu",
 ]

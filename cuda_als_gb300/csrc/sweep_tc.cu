@@ -33,204 +33,16 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 
 #include "handle.h"
 #include "internal.h"
-#include "regsolve.cuh"
-#include "solvers.cuh"
+#include "sweep_tc_kernel.cuh"
 #include "tc.h"
 
 namespace als {
 namespace tcg {
-
-constexpr int KC = 64;                       // ratings per stage
-constexpr int NSTAGE = 4;
-constexpr int LAG = NSTAGE - 1;              // stages of copies in flight per producer lane
-constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
-constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
-constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
-constexpr int R_BYTES = 2 * ATOM_BYTES;      // K-major rating tile, N = 16 rows x 64 ratings
-constexpr int STAGE_BYTES = TILE_BYTES + R_BYTES;
-constexpr int MAXF = 128;
-constexpr int MAX_NBUF = 4;
-constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
-
-struct Meta {  // per stage / per accumulator
-    int32_t row;    // -1 = end of work
-    int32_t cnt;    // ratings in this stage
-    int32_t flags;  // 1 = first stage of the row, 2 = last stage of the row
-    int32_t nu;     // ratings of the row
-};
-
-struct Params {
-    const int32_t *ptr, *idx, *order;
-    const float *val;
-    const __nv_bfloat16 *Ybf;  // (n_opp + 1) x fst, row n_opp all zero
-    float *X;                  // this side's FP32 factors (in: CG warm start, out: solution)
-    int32_t *work;             // atomic row counter (zeroed before the launch)
-    int32_t *flags;            // [0] flagged rows, [1] FP64-refined rows, [2] timeouts
-    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, nepi, solve, cg_iters;
-    int32_t refine_steps;
-    float lambda, cg_tol, cond_threshold;
-};
-
-// Per-warpgroup shared scratch: L rows (or the FP32 Gram for the shared-memory LU), vectors.
-template <int FP>
-struct GroupSmem {
-    static constexpr int LS = FP + 4;
-    static constexpr size_t ls_floats = (size_t)FP * LS;
-    static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
-};
-
-struct Geometry {
-    int fp, fst, ng, acc_stride, tmem_cols, nbuf, nepi, nthreads;
-    size_t smem;
-};
-
-__host__ __device__ inline int gs_of(int f) { return (f + 1) % 2 ? f + 1 : f + 2; }
-
-inline int fp_of(int f) {
-    const int r = (f + 15) / 16 * 16;
-    return r <= 32 ? 32 : r <= 64 ? 64 : r <= 112 ? 112 : 128;
-}
-
-inline size_t group_floats(int fp) {
-    switch (fp) {
-    case 32: return GroupSmem<32>::floats;
-    case 64: return GroupSmem<64>::floats;
-    case 112: return GroupSmem<112>::floats;
-    default: return GroupSmem<128>::floats;
-    }
-}
-
-inline Geometry geometry(int f) {
-    Geometry g;
-    g.fp = fp_of(f);
-    g.fst = (f + 7) / 8 * 8;
-    g.ng = (f + 15) / 16 * 16;
-    const int acc_cols = g.ng + 16;
-    g.acc_stride = acc_cols <= 128 ? 128 : 256;
-    g.nbuf = acc_cols <= 128 ? 4 : 2;
-    g.nepi = g.nbuf / 2;
-    g.tmem_cols = g.nbuf * g.acc_stride;
-    g.nthreads = 64 + 128 * g.nepi;
-    size_t bytes = (size_t)NSTAGE * STAGE_BYTES;                     // operand ring
-    bytes += sizeof(float) * group_floats(g.fp) * g.nepi;            // per-group scratch
-    bytes += sizeof(int32_t) * NSTAGE * KC;                          // gathered column ids
-    bytes += 1024;                                                   // metas, barriers, scalars
-    g.smem = bytes + 1024;                                           // 1024-B alignment slack
-    return g;
-}
-
-// ---------------------------------------------------------------------------------- PTX helpers
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ unsigned long long now_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait; false on timeout or (when abort != nullptr) once another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
-    if (mbar_try(bar, parity)) return true;
-    const unsigned long long t0 = now_ns();
-    for (uint32_t i = 0;; ++i) {
-        if (mbar_try(bar, parity)) return true;
-        if ((i & 255) == 255) {
-            if (abort && *abort) return false;
-            if (now_ns() - t0 > WAIT_NS) return false;
-        }
-    }
-}
-// Warp-uniform wait: lane 0 waits, the outcome is broadcast (no lane can diverge on a timeout).
-__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort) {
-    int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort) ? 1 : 0;
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
-}
-__device__ __forceinline__ void fence_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor, SWIZZLE_128B, sm_100 layout (version 1 at bits 46-47).
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
-    return d;
-}
-
-// Instruction descriptor of tcgen05.mma kind::f16: D F32, A/B BF16, majors, N, M.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N, bool a_mn, bool b_mn) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) |
-           ((b_mn ? 1u : 0u) << 16) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-        : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-        "%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// ------------------------------------------------------------------------------------- kernels
 
 __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, int f, int fst,
                                      __nv_bfloat16 *__restrict__ out) {
@@ -243,379 +55,9 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
     }
 }
 
-// sum_j D[i][j] x_j re-read from TMEM in 16-column chunks (FP64 products and sums when WIDE)
-template <int FP, bool WIDE>
-__device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *xs) {
-    double acc = 0.0;
-    float accf = 0.f;
-#pragma unroll
-    for (int c = 0; c < FP; c += 16) {
-        if (c < ng) {
-            float v[16];
-            tmem_ld16(tb + c, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                if (WIDE)
-                    acc = fma((double)v[j], (double)xs[c + j], acc);
-                else
-                    accf = fmaf(v[j], xs[c + j], accf);
-            }
-        }
-    }
-    return WIDE ? acc : (double)accf;
-}
-
-// The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
-template <int FP>
-__device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
-                          float *gsm, const GroupSync &gs) {
-    float *Ls = gsm;
-    float *sv = gsm + GroupSmem<FP>::ls_floats;
-    float *yv = sv + FP;
-    float *red = yv + FP;
-    float *vec = red + 16;  // 5 x 128 floats for the shared-memory solvers
-    const int f = p.f;
-    float *xo = p.X + (int64_t)m.row * f;
-    const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
-
-    float a[FP];
-#pragma unroll
-    for (int c = 0; c < FP; c += 16) {
-        if (c < p.ng) {
-            tmem_ld16(tb + c, &a[c]);
-        } else {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) a[c + j] = 0.f;
-        }
-    }
-    float bi;
-    {
-        float v[16];
-        tmem_ld16(tb + p.ng, v);
-        bi = i < f ? v[0] : 0.f;
-    }
-#pragma unroll
-    for (int j = 0; j < FP; ++j)
-        if (j == i) a[j] = i < f ? a[j] + reg : 1.f;  // identity on the padded rows
-
-    int slot = 0;
-    float xi = 0.f;
-    bool good = true;
-    if (p.solve == ALS_SOLVE_CG_FP32 || p.solve == ALS_SOLVE_CG_FP16) {
-        xi = cg_reg<FP>(a, bi, i < f ? xo[i] : 0.f, i, sv, red, p.cg_iters, p.cg_tol, gs);
-    } else if (p.solve == ALS_SOLVE_LU) {
-        // reference semantics: LU without pivoting of the full matrix, in shared memory
-        const int GS = gs_of(f);
-        float *G = Ls;
-        if (i < f) {
-#pragma unroll
-            for (int j = 0; j < FP; ++j)
-                if (j < f) G[i * GS + j] = a[j];
-        }
-        float *vb = vec;
-        if (i < f) vb[i] = bi;
-        gs.sync();
-        if (g == 0)
-            good = lu_nopivot_solve<NamedSync<1, 128>>(G, GS, f, vb, et, 128);
-        else
-            good = lu_nopivot_solve<NamedSync<2, 128>>(G, GS, f, vb, et, 128);
-        xi = i < f ? vb[i] : 0.f;
-        gs.sync();
-    } else {
-        // Cholesky (+ refinement against the TMEM copy of A)
-        good = chol_reg<FP>(a, i, Ls, gs);
-        const float bad = gsum128(good ? 0.f : 1.f, red, slot, gs);
-        good = bad == 0.f;
-        if (good) {
-            xi = chol_solve_reg<FP>(a, bi, i, Ls, yv, gs);
-            // condition estimate from the Cholesky diagonal: (max L_ii / min L_ii)^2
-            float lii = 1.f;
-#pragma unroll
-            for (int j = 0; j < FP; ++j)
-                if (j == i) lii = a[j];
-            const float dmax = gmax128(i < f ? lii : 0.f, red, slot, gs);
-            const float dmin = -gmax128(i < f ? -lii : -3.0e38f, red, slot, gs);
-            const bool wide = (dmax / dmin) * (dmax / dmin) > p.cond_threshold;
-            for (int s = 0; s < p.refine_steps; ++s) {
-                if (i < FP) sv[i] = i < f ? xi : 0.f;
-                gs.sync();
-                const double ax = wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
-                                       : tmem_rowdot<FP, false>(tb, p.ng, sv);
-                float ri;
-                if (wide)
-                    ri = (float)((double)bi - ax - (double)reg * (double)xi);
-                else
-                    ri = bi - (float)ax - reg * xi;
-                if (i >= f) ri = 0.f;
-                const float di = chol_solve_reg<FP>(a, ri, i, Ls, yv, gs);
-                xi += di;
-            }
-            if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
-        }
-    }
-    const float nonfinite = gsum128((i < f && !isfinite(xi)) ? 1.f : 0.f, red, slot, gs);
-    if (!good || nonfinite > 0.f) {
-        if (i < f) xo[i] = 0.f;
-        if (et == 0) atomicAdd(&p.flags[0], 1);
-    } else if (i < f) {
-        xo[i] = xi;
-    }
-}
-
-template <int FP>
-__global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *ring = smem;
-    float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
-    int32_t *scol = (int32_t *)(gscratch + GroupSmem<FP>::floats * p.nepi);
-    Meta *smeta = (Meta *)(((uintptr_t)(scol + NSTAGE * KC) + 15) & ~(uintptr_t)15);
-    Meta *ameta = smeta + NSTAGE;
-    uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
-    uint64_t *full = bars, *empty = bars + NSTAGE;
-    uint64_t *acc_full = bars + 2 * NSTAGE;
-    uint64_t *acc_empty = acc_full + MAX_NBUF, *acc_meta = acc_empty + MAX_NBUF;
-    uint64_t *drain = acc_meta + MAX_NBUF;
-    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
-    volatile int *abort = (volatile int *)(tmem_slot + 1);
-    volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nbuf = 2 * p.nepi;
-
-    // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
-    for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += blockDim.x)
-        reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
-    if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) {
-            mbar_init(smem_u32(&full[s]), 1);
-            mbar_init(smem_u32(&empty[s]), 1);
-        }
-        for (int b = 0; b < MAX_NBUF; ++b) {
-            mbar_init(smem_u32(&acc_full[b]), 1);
-            mbar_init(smem_u32(&acc_empty[b]), 1);
-            mbar_init(smem_u32(&acc_meta[b]), 1);
-        }
-        mbar_init(smem_u32(drain), 1);
-        *abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    fence_async_smem();
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                         smem_u32(tmem_slot)),
-                     "r"(p.tmem_cols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem_base = *tmem_slot;
-
-    if (warp == 0) {
-        // ------------------------------------------------------------------ producer
-        const int nchunk = p.fst / 8;
-        const char *ybytes = reinterpret_cast<const char *>(p.Ybf);
-        uint32_t it = 0;        // stage counter
-        uint32_t pending = 0;   // stages whose copies are issued but not yet signalled
-        bool ok = true;
-        auto signal_oldest = [&](uint32_t stage_it) {
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&full[stage_it % NSTAGE]));
-        };
-        while (ok) {
-            int slot = 0;
-            if (lane == 0) slot = atomicAdd(p.work, 1);
-            slot = __shfl_sync(0xffffffffu, slot, 0);
-            const bool done = slot >= p.nrows;
-            const int row = done ? -1 : p.order[slot];
-            const int beg = done ? 0 : p.ptr[row], end = done ? 0 : p.ptr[row + 1];
-            const int nu = end - beg;
-            int base = beg;
-            do {  // at least one stage per row (an empty row or the end marker is one stage)
-                const int cnt = done ? 0 : min(KC, end - base);
-                const int s = it % NSTAGE;
-                if (it >= NSTAGE &&
-                    !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
-                    ok = false;
-                    break;
-                }
-                uint8_t *tile = ring + s * STAGE_BYTES;
-                uint8_t *rt = tile + TILE_BYTES;
-                const int cnt16 = (cnt + 15) & ~15;
-                for (int k = lane; k < KC; k += 32) {
-                    const int c = k < cnt ? p.idx[base + k] : p.zero_row;
-                    scol[s * KC + k] = c;
-                    const float r = k < cnt ? p.val[base + k] : 0.f;
-                    reinterpret_cast<__nv_bfloat16 *>(rt)[k] = __float2bfloat16_rn(r);
-                }
-                __syncwarp();
-                const uint32_t tile_s = smem_u32(tile);
-                for (int e = lane; e < cnt16 * nchunk; e += 32) {
-                    const int k = e / nchunk, c = e - k * nchunk;
-                    const int col = scol[s * KC + k];
-                    const uint32_t dst = tile_s + (c >> 3) * ATOM_STRIDE + (k >> 3) * ATOM_BYTES +
-                                         (k & 7) * 128 + (((c & 7) ^ (k & 7)) << 4);
-                    cp_async16(dst, ybytes + ((size_t)col * p.fst + (size_t)c * 8) * 2);
-                }
-                cp_commit();
-                if (lane == 0) {
-                    Meta m;
-                    m.row = row;
-                    m.cnt = cnt;
-                    m.flags = (base == beg ? 1 : 0) | (done || base + KC >= end ? 2 : 0);
-                    m.nu = nu;
-                    smeta[s] = m;
-                }
-                ++pending;
-                if (pending > LAG) {
-                    cp_wait<LAG>();
-                    signal_oldest(it - LAG);
-                    --pending;
-                }
-                ++it;
-                base += KC;
-            } while (!done && base < end);
-            if (done) break;
-        }
-        cp_wait<0>();
-        while (pending > 0) {  // signal what is still in flight, oldest first
-            signal_oldest(it - pending);
-            --pending;
-        }
-        if (!ok) {
-            *abort = 1;
-            if (lane == 0) atomicAdd(&p.flags[2], 1);
-        }
-    } else if (warp == 1) {
-        // ------------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            const uint32_t idesc_g = idesc_bf16(128, p.ng, true, true);
-            const uint32_t idesc_r = idesc_bf16(128, 16, true, false);
-            const uint32_t ring_s = smem_u32(ring);
-            uint32_t it = 0, acc_it = 0, buf = 0;
-            bool ok = true;
-            auto take_buffer = [&]() -> bool {  // wait until accumulator acc_it % nbuf is free
-                buf = acc_it % nbuf;
-                const uint32_t use = acc_it / nbuf;
-                if (use >= 1 && !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort))
-                    return false;
-                tc_fence_after();
-                return true;
-            };
-            for (;;) {
-                const int s = it % NSTAGE;
-                if (!mbar_wait(smem_u32(&full[s]), (it / NSTAGE) & 1, abort)) { ok = false; break; }
-                fence_async_smem();
-                tc_fence_after();
-                const Meta m = smeta[s];
-                if (m.row < 0) {  // end of work: one end marker per solver warpgroup
-                    for (int g = 0; g < p.nepi && ok; ++g) {
-                        if (!take_buffer()) { ok = false; break; }
-                        ameta[buf] = m;
-                        mbar_arrive(smem_u32(&acc_meta[buf]));
-                        ++acc_it;
-                    }
-                    break;
-                }
-                if ((m.flags & 1) && !take_buffer()) { ok = false; break; }
-                const uint32_t dg = tmem_base + buf * p.acc_stride;
-                const uint32_t db = dg + p.ng;
-                const uint32_t tile_s = ring_s + s * STAGE_BYTES;
-                const int nk = (m.cnt + 15) >> 4;
-                for (int kk = 0; kk < nk; ++kk) {
-                    const uint64_t ad = sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
-                    const uint64_t rd = sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
-                    const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
-                    mma_bf16(dg, ad, ad, idesc_g, accum);
-                    mma_bf16(db, ad, rd, idesc_r, accum);
-                }
-                mma_commit(smem_u32(&empty[s]));
-                if (m.flags & 2) {
-                    ameta[buf] = m;
-                    if (m.nu > 0) mma_commit(smem_u32(&acc_full[buf]));
-                    mbar_arrive(smem_u32(&acc_meta[buf]));
-                    ++acc_it;
-                }
-                ++it;
-            }
-            // drain: every MMA issued so far has completed before TMEM is released
-            mma_commit(smem_u32(drain));
-            if (!mbar_wait(smem_u32(drain), 0, nullptr)) ok = false;
-            if (!ok) {
-                *abort = 1;
-                atomicAdd(&p.flags[2], 1);
-            }
-        }
-        __syncwarp();
-    } else if (warp < 2 + 4 * p.nepi) {
-        // ------------------------------------------------------------------ solver warpgroups
-        const int g = (warp - 2) >> 2;
-        const int et = tid - 64 - 128 * g;           // 0..127 inside the group
-        const int lanegrp = (warp & 3) * 32;         // TMEM lanes this warp may read
-        const int i = lanegrp + lane;                // row of the Gram held by this thread
-        const GroupSync gs{1 + g};
-        float *gsm = gscratch + GroupSmem<FP>::floats * g;
-        volatile int *okflag = grp_ok + g;
-        uint32_t fullcnt[2] = {0, 0};
-        bool ok = true;
-        auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
-            if (et == 0) *okflag = mbar_wait(bar, parity, abort) ? 1 : 0;
-            gs.sync();
-            const bool r = *okflag != 0;
-            gs.sync();
-            return r;
-        };
-        for (uint32_t acc_it = g;; acc_it += p.nepi) {
-            const uint32_t buf = acc_it % nbuf;
-            const uint32_t use = acc_it / nbuf;
-            const int lb = (int)(buf / p.nepi);      // 0/1: this group's two buffers
-            if (!group_wait(smem_u32(&acc_meta[buf]), use & 1)) { ok = false; break; }
-            const Meta m = ameta[buf];
-            if (m.row < 0) break;
-            if (m.nu > 0) {
-                if (!group_wait(smem_u32(&acc_full[buf]), fullcnt[lb] & 1)) { ok = false; break; }
-                ++fullcnt[lb];
-                tc_fence_after();
-                const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
-                solve_row<FP>(p, m, tb, i, et, g, gsm, gs);
-            } else if (i < p.f) {
-                p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
-            }
-            tc_fence_before();
-            gs.sync();
-            if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
-        }
-        if (!ok) {
-            *abort = 1;
-            if (et == 0) atomicAdd(&p.flags[2], 1);
-        }
-    }
-
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 1)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
-                     "r"(p.tmem_cols)
-                     : "memory");
-}
-
-template <int FP>
-cudaError_t configure(size_t smem) {
-    return cudaFuncSetAttribute(sweep_tc_kernel<FP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
-}
-
-template <int FP>
-void launch(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
-    sweep_tc_kernel<FP><<<grid, g.nthreads, g.smem, st>>>(p);
-}
-
 }  // namespace tcg
 }  // namespace als
+
 
 // ------------------------------------------------------------------------------------- host side
 
@@ -666,10 +108,10 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     for (int k = 0; k < 2; ++k) cudaEventCreate(&t->ev_q[k]);
     cudaError_t e;
     switch (t->geo.fp) {
-    case 32: e = tcg::configure<32>(t->geo.smem); break;
-    case 64: e = tcg::configure<64>(t->geo.smem); break;
-    case 112: e = tcg::configure<112>(t->geo.smem); break;
-    default: e = tcg::configure<128>(t->geo.smem); break;
+    case 32: e = tcg::configure_32(t->geo.smem); break;
+    case 64: e = tcg::configure_64(t->geo.smem); break;
+    case 112: e = tcg::configure_112(t->geo.smem); break;
+    default: e = tcg::configure_128(t->geo.smem); break;
     }
     if (e != cudaSuccess) {
         *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
@@ -726,7 +168,12 @@ als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *wh
     p.acc_stride = t->geo.acc_stride;
     p.tmem_cols = t->geo.tmem_cols;
     p.nepi = t->geo.nepi;
-    p.solve = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
+    switch (h->cfg.solve_type) {
+    case ALS_SOLVE_CG_FP32:
+    case ALS_SOLVE_CG_FP16: p.solve = tcg::SOLVER_CG; break;
+    case ALS_SOLVE_LU: p.solve = tcg::SOLVER_LU; break;
+    default: p.solve = tcg::SOLVER_CHOL; break;
+    }
     p.cg_iters = h->cfg.cg_steps;
     p.refine_steps = h->cfg.refine_steps;
     p.lambda = h->cfg.lambda;
@@ -734,10 +181,10 @@ als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *wh
     p.cond_threshold = h->cfg.cond_threshold;
     const int grid = (int)std::min<int64_t>(rows, t->num_sms);
     switch (t->geo.fp) {
-    case 32: tcg::launch<32>(p, t->geo, grid, st); break;
-    case 64: tcg::launch<64>(p, t->geo, grid, st); break;
-    case 112: tcg::launch<112>(p, t->geo, grid, st); break;
-    default: tcg::launch<128>(p, t->geo, grid, st); break;
+    case 32: tcg::launch_32(p, t->geo, grid, st); break;
+    case 64: tcg::launch_64(p, t->geo, grid, st); break;
+    case 112: tcg::launch_112(p, t->geo, grid, st); break;
+    default: tcg::launch_128(p, t->geo, grid, st); break;
     }
     ++*launches;
     cudaError_t e = cudaGetLastError();

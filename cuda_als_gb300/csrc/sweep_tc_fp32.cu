@@ -1,0 +1,12 @@
+// sweep_tc_fp32.cu — instantiation of the tcgen05 half-sweep for padded size 32 (its own
+// translation unit so the variants compile in parallel).
+#include "sweep_tc_kernel.cuh"
+
+namespace als {
+namespace tcg {
+cudaError_t configure_32(size_t smem) { return configure_fp<32>(smem); }
+void launch_32(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
+    launch_fp<32>(p, g, grid, st);
+}
+}  // namespace tcg
+}  // namespace als
