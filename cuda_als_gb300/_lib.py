@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
                                         C.POINTER(f64)], i32),
         "als_csr_to_csc": ([C.POINTER(CsrView), P, P, P], i32),
         "als_csr_to_csc_device": ([C.POINTER(CsrView), P, P, P, P], i32),
+        "als_csr_to_csc_device_noalloc": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_degree_order": ([i64, P, P], i32),
         "als_synth_shape": ([i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                              C.POINTER(i32), C.POINTER(f32)], i32),
@@ -109,5 +110,6 @@ EXPORTS = [
     "als_get_factors", "als_set_factors", "als_get_device_factors", "als_save_libmf",
     "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan",
     "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
+    "als_csr_to_csc_device_noalloc",
     "als_degree_order", "als_synth_shape", "als_synth_generate",
 ]

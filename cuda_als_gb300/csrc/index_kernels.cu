@@ -11,6 +11,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <string>
+
 #include "internal.h"
 
 namespace als {
@@ -397,4 +400,82 @@ cudaError_t count_bad_entries(int64_t nnz, const int32_t *idx, int32_t limit, co
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------------------
+// CSR -> CSC without any allocation, for callers that may not allocate device memory.
+//
+// Some callers cannot call cudaMalloc (or have torch or any other allocator do it for them):
+// code that runs while a stream is being captured into a CUDA graph in the global capture mode,
+// where an allocation invalidates the capture; plug-ins hosted by an engine that owns all device
+// memory and forbids allocations inside its callbacks; and latency-critical loops that must not
+// synchronise on the allocator.  For them the transpose's scratch lives in one file-scope device
+// array of NOALLOC_SCRATCH_BYTES (16 MiB), which every GPU that loads this library holds until the
+// process exits.  That bounds the input to about 590,000 ratings; larger inputs are rejected with
+// ALS_ERR_INVALID_ARG before anything runs.
+//
+// In host code the array's name is only a host-side stand-in, so the device address is looked up
+// once per device with cudaGetSymbolAddress (with that device current) on the first call made on
+// it; make that first call before any stream capture begins.  Every call shares the one array:
+// calls whose work overlaps on the GPU (different streams, or several threads) race on it and
+// must be serialised by the caller.  The transpose writes every scratch word before it reads it,
+// so no clearing is needed between calls.
+// ---------------------------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+}  // namespace
+
 }  // namespace als
+
+extern "C" als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int32_t *col_ptrs,
+                                                    int32_t *row_idxs, float *vals,
+                                                    void *stream) {
+    using namespace als;
+    if (!csr || !col_ptrs || !csr->row_ptrs ||
+        (csr->nnz > 0 && (!row_idxs || !vals || !csr->col_idxs || !csr->vals)))
+        return set_global_error(ALS_ERR_INVALID_ARG, "null argument");
+    if (csr->rows < 0 || csr->cols < 0 || csr->nnz < 0 || csr->nnz > INT32_MAX ||
+        csr->rows >= INT32_MAX || csr->cols >= INT32_MAX)
+        return set_global_error(ALS_ERR_INVALID_ARG, "shape out of range");
+    const size_t need = transpose_scratch_bytes(csr->rows, csr->cols, csr->nnz);
+    if (need > NOALLOC_SCRATCH_BYTES)
+        return set_global_error(
+            ALS_ERR_INVALID_ARG,
+            "als_csr_to_csc_device_noalloc: " + std::to_string(csr->nnz) +
+                " ratings need " + std::to_string(need) + " bytes of scratch, more than its fixed " +
+                std::to_string(NOALLOC_SCRATCH_BYTES) + "-byte array; use als_csr_to_csc_device");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return set_global_error(ALS_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return set_global_error(ALS_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {  // set-up, once per device, with that device current
+            void *addr = nullptr;
+            e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+            if (e != cudaSuccess || !addr)
+                return set_global_error(ALS_ERR_CUDA,
+                                        std::string("cudaGetSymbolAddress: ") +
+                                            cudaGetErrorString(e));
+            g_noalloc_addr[dev] = addr;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    e = csr_to_csc_device(csr->rows, csr->cols, csr->nnz, csr->row_ptrs, csr->col_idxs,
+                          csr->vals, col_ptrs, row_idxs, vals, scratch, (cudaStream_t)stream,
+                          nullptr, nullptr);
+    if (e != cudaSuccess)
+        return set_global_error(ALS_ERR_CUDA, std::string("csr_to_csc: ") + cudaGetErrorString(e));
+    return ALS_OK;
+}
+
