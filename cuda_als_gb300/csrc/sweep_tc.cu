@@ -63,8 +63,18 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
 
 using namespace als;
 
+static int tcg_solver(int solve_type) {
+    switch (solve_type) {
+    case ALS_SOLVE_CG_FP32:
+    case ALS_SOLVE_CG_FP16: return tcg::SOLVER_CG;
+    case ALS_SOLVE_LU: return tcg::SOLVER_LU;
+    default: return tcg::SOLVER_CHOL;
+    }
+}
+
 struct TcState {
     tcg::Geometry geo{};
+    int solver = 1;
     __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
     int32_t *d_work = nullptr;
     int num_sms = 0;
@@ -90,7 +100,8 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     }
     TcState *t = new TcState();
     h->tc = t;
-    t->geo = tcg::geometry(h->f);
+    t->solver = tcg_solver(h->cfg.solve_type);
+    t->geo = tcg::geometry(h->f, t->solver);
     t->num_sms = sms;
     const int64_t opp[2] = {h->n, h->m};  // side 0 gathers V rows, side 1 gathers U rows
     for (int s = 0; s < 2; ++s) {
@@ -168,12 +179,7 @@ als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *wh
     p.acc_stride = t->geo.acc_stride;
     p.tmem_cols = t->geo.tmem_cols;
     p.nepi = t->geo.nepi;
-    switch (h->cfg.solve_type) {
-    case ALS_SOLVE_CG_FP32:
-    case ALS_SOLVE_CG_FP16: p.solve = tcg::SOLVER_CG; break;
-    case ALS_SOLVE_LU: p.solve = tcg::SOLVER_LU; break;
-    default: p.solve = tcg::SOLVER_CHOL; break;
-    }
+    p.solve = t->solver;
     p.cg_iters = h->cfg.cg_steps;
     p.refine_steps = h->cfg.refine_steps;
     p.lambda = h->cfg.lambda;

@@ -14,8 +14,10 @@ namespace als {
 namespace tcg {
 
 constexpr int KC = 64;                       // ratings per stage
-constexpr int NSTAGE = 4;
-constexpr int LAG = NSTAGE - 1;              // stages of copies in flight per producer lane
+constexpr int MAX_NSTAGE = 8;
+// Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
+// gathered bytes in flight per SM); the Cholesky / LU scratch leaves room for five stages.
+__host__ __device__ constexpr int nstage_of(int solver) { return solver == 0 ? 8 : 5; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
@@ -45,11 +47,17 @@ struct Params {
     float lambda, cg_tol, cond_threshold;
 };
 
-// Per-warpgroup shared scratch: L rows (or the FP32 Gram for the shared-memory LU), vectors.
+// Per-warpgroup shared scratch: L rows (or the FP32 Gram for the shared-memory LU) unless the
+// solver is CG, then two vectors, the reduction ring and the shared-memory solvers' vectors.
 template <int FP>
 struct GroupSmem {
     static constexpr int LS = FP + 4;
     static constexpr size_t ls_floats = (size_t)FP * LS;
+    static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
+};
+template <int FP, int SOLVER>
+struct GroupLayout {
+    static constexpr size_t ls_floats = SOLVER == 0 ? 0 : GroupSmem<FP>::ls_floats;
     static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
@@ -65,16 +73,12 @@ inline int fp_of(int f) {
     return r <= 32 ? 32 : r <= 64 ? 64 : r <= 112 ? 112 : 128;
 }
 
-inline size_t group_floats(int fp) {
-    switch (fp) {
-    case 32: return GroupSmem<32>::floats;
-    case 64: return GroupSmem<64>::floats;
-    case 112: return GroupSmem<112>::floats;
-    default: return GroupSmem<128>::floats;
-    }
+inline size_t group_floats(int fp, int solver) {
+    const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
+    return solver == 0 ? vec : (size_t)fp * (fp + 4) + vec;
 }
 
-inline Geometry geometry(int f) {
+inline Geometry geometry(int f, int solver) {
     Geometry g;
     g.fp = fp_of(f);
     g.fst = (f + 7) / 8 * 8;
@@ -85,9 +89,10 @@ inline Geometry geometry(int f) {
     g.nepi = g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
     g.nthreads = 64 + 128 * g.nepi;
-    size_t bytes = (size_t)NSTAGE * STAGE_BYTES;                     // operand ring
-    bytes += sizeof(float) * group_floats(g.fp) * g.nepi;            // per-group scratch
-    bytes += sizeof(int32_t) * NSTAGE * KC;                          // gathered column ids
+    const int ns = nstage_of(solver);
+    size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
+    bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
+    bytes += sizeof(int32_t) * ns * KC;                              // gathered column ids
     bytes += 1024;                                                   // metas, barriers, scalars
     g.smem = bytes + 1024;                                           // 1024-B alignment slack
     return g;
@@ -229,7 +234,7 @@ template <int FP, int SOLVER>
 __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
                           float *gsm, const GroupSync &gs) {
     float *Ls = gsm;
-    float *sv = gsm + GroupSmem<FP>::ls_floats;
+    float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
     float *red = yv + FP;
     float *vec = red + 16;  // 5 x 128 floats for the shared-memory solvers
@@ -323,11 +328,13 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 
 template <int FP, int SOLVER>
 __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
+    constexpr int NSTAGE = nstage_of(SOLVER);
+    constexpr int LAG = NSTAGE - 1;  // stages of copies in flight per producer lane
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
     float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
-    int32_t *scol = (int32_t *)(gscratch + GroupSmem<FP>::floats * p.nepi);
+    int32_t *scol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * p.nepi);
     Meta *smeta = (Meta *)(((uintptr_t)(scol + NSTAGE * KC) + 15) & ~(uintptr_t)15);
     Meta *ameta = smeta + NSTAGE;
     uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
@@ -422,25 +429,37 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
             int nbase, ncnt;
             grab(nbase, ncnt);
             const int nrow = lane < ncnt ? p.order[nbase + lane] : 0;
+            // stage cursors t (j, base), t+1 (j1, b1) with their column ids / ratings in flight;
+            // t+2 is loaded while t is issued
+            auto advance = [&](int jj, int bb, int &jo, int &bo) {
+                const int e = __shfl_sync(0xffffffffu, cend, jj);
+                jo = jj;
+                bo = bb + KC;
+                if (bo >= e) {
+                    ++jo;
+                    bo = jo < ccnt ? __shfl_sync(0xffffffffu, cbeg, jo < ccnt ? jo : 0) : 0;
+                }
+            };
             int j = 0;
             int base = __shfl_sync(0xffffffffu, cbeg, 0);
             int c0, c1;
             float v0, v1;
             stage_load(0, base, c0, c1, v0, v1);
+            int j1, b1;
+            advance(j, base, j1, b1);
+            int d0 = 0, d1 = 0;
+            float w0 = 0.f, w1 = 0.f;
+            if (j1 < ccnt) stage_load(j1, b1, d0, d1, w0, w1);
             while (j < ccnt) {
                 const int row = __shfl_sync(0xffffffffu, crow, j);
                 const int beg = __shfl_sync(0xffffffffu, cbeg, j);
                 const int end = __shfl_sync(0xffffffffu, cend, j);
                 const int cnt = min(KC, end - base);
-                // next stage cursor and its prefetch
-                int nj = j, nbs = base + KC;
-                if (nbs >= end) {
-                    ++nj;
-                    nbs = nj < ccnt ? __shfl_sync(0xffffffffu, cbeg, nj < ccnt ? nj : 0) : 0;
-                }
+                int j2 = ccnt, b2 = 0;
+                if (j1 < ccnt) advance(j1, b1, j2, b2);
                 int pc0 = 0, pc1 = 0;
                 float pv0 = 0.f, pv1 = 0.f;
-                if (nj < ccnt) stage_load(nj, nbs, pc0, pc1, pv0, pv1);
+                if (j2 < ccnt) stage_load(j2, b2, pc0, pc1, pv0, pv1);
 
                 const int s = it % NSTAGE;
                 if (it >= NSTAGE &&
@@ -486,12 +505,18 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
                     --pending;
                 }
                 ++it;
-                j = nj;
-                base = nbs;
-                c0 = pc0;
-                c1 = pc1;
-                v0 = pv0;
-                v1 = pv1;
+                j = j1;
+                base = b1;
+                c0 = d0;
+                c1 = d1;
+                v0 = w0;
+                v1 = w1;
+                j1 = j2;
+                b1 = b2;
+                d0 = pc0;
+                d1 = pc1;
+                w0 = pv0;
+                w1 = pv1;
             }
             // switch to the next chunk
             cbase = nbase;
@@ -596,7 +621,7 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
         const int lanegrp = (warp & 3) * 32;         // TMEM lanes this warp may read
         const int i = lanegrp + lane;                // row of the Gram held by this thread
         const GroupSync gs{1 + g};
-        float *gsm = gscratch + GroupSmem<FP>::floats * g;
+        float *gsm = gscratch + GroupLayout<FP, SOLVER>::floats * g;
         volatile int *okflag = grp_ok + g;
         uint32_t fullcnt[2] = {0, 0};
         bool ok = true;
@@ -646,14 +671,19 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
 // limit of the three solver variants and launch the selected one.
 template <int FP>
 cudaError_t configure_fp(size_t smem) {
+    // every variant may use up to the device's opt-in maximum; each launch asks for its own size
+    int dev = 0, maxsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((size_t)maxsm < smem) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CG>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CHOL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_LU>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     return e;
 }
 
