@@ -219,7 +219,8 @@ static void group_heldout(int64_t m, int64_t nh, const int32_t *hrow, int64_t *h
 static double adjoint_impl(int64_t m, int64_t n, int f, double lambda, const int32_t *ptr,
                            const int32_t *idx, const float *val, const double *Y, int64_t nh,
                            const int32_t *hrow, const int32_t *hcol, const float *hval,
-                           double *X, double *dLdY, double *dLdlambda, int nthreads) {
+                           double *X, double *dLdY, double *dLdlambda, int nthreads,
+                           const uint8_t *row_mask) {
     int64_t *hptr = (int64_t *)malloc(sizeof(int64_t) * (size_t)(m + 1));
     int64_t *hperm = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nh > 0 ? nh : 1));
     group_heldout(m, nh, hrow, hptr, hperm);
@@ -239,6 +240,7 @@ static double adjoint_impl(int64_t m, int64_t n, int f, double lambda, const int
         double *grad = want_grad ? (double *)calloc((size_t)(n * f), sizeof(double)) : NULL;
 #pragma omp for schedule(dynamic, 16)
         for (int64_t u = 0; u < m; ++u) {
+            if (row_mask && !row_mask[u]) continue;
             int64_t beg = ptr[u], end = ptr[u + 1];
             if (end == beg) {
                 for (int i = 0; i < f; ++i) x[i] = 0.0;
@@ -306,7 +308,7 @@ double oracle_user_adjoint(int64_t m, int64_t n, int f, double lambda, const int
                            const float *hval, double *X, double *dLdY, double *dLdlambda,
                            int nthreads) {
     return adjoint_impl(m, n, f, lambda, ptr, idx, val, Y, nh, hrow, hcol, hval, X, dLdY,
-                        dLdlambda, nthreads);
+                        dLdlambda, nthreads, NULL);
 }
 
 double oracle_user_loss(int64_t m, int64_t n, int f, double lambda, const int32_t *ptr,
@@ -314,5 +316,16 @@ double oracle_user_loss(int64_t m, int64_t n, int f, double lambda, const int32_
                         const int32_t *hrow, const int32_t *hcol, const float *hval,
                         int nthreads) {
     return adjoint_impl(m, n, f, lambda, ptr, idx, val, Y, nh, hrow, hcol, hval, NULL, NULL,
-                        NULL, nthreads);
+                        NULL, nthreads, NULL);
+}
+
+/* The part of the held-out loss contributed by the rows with row_mask[u] != 0: the only terms
+ * that depend on y_i are those of rows that rated i or hold i out, which makes central
+ * differences at full size cheap. */
+double oracle_user_loss_rows(int64_t m, int64_t n, int f, double lambda, const int32_t *ptr,
+                             const int32_t *idx, const float *val, const double *Y, int64_t nh,
+                             const int32_t *hrow, const int32_t *hcol, const float *hval,
+                             const uint8_t *row_mask, int nthreads) {
+    return adjoint_impl(m, n, f, lambda, ptr, idx, val, Y, nh, hrow, hcol, hval, NULL, NULL,
+                        NULL, nthreads, row_mask);
 }

@@ -68,6 +68,12 @@ double oracle_user_loss(int64_t m, int64_t n, int f, double lambda, const int32_
                         const int32_t *hrow, const int32_t *hcol, const float *hval,
                         int nthreads);
 
+/* The held-out loss restricted to rows with row_mask[u] != 0 (for central differences). */
+double oracle_user_loss_rows(int64_t m, int64_t n, int f, double lambda, const int32_t *ptr,
+                             const int32_t *idx, const float *val, const double *Y, int64_t nh,
+                             const int32_t *hrow, const int32_t *hcol, const float *hval,
+                             const uint8_t *row_mask, int nthreads);
+
 /* omp_get_max_threads() of this build (1 without OpenMP) */
 int oracle_max_threads(void);
 

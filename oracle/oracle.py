@@ -37,6 +37,8 @@ def lib():
         L.oracle_user_adjoint.restype = dbl
         L.oracle_user_loss.argtypes = [i64, i64, i32, dbl, P, P, P, P, i64, P, P, P, i32]
         L.oracle_user_loss.restype = dbl
+        L.oracle_user_loss_rows.argtypes = [i64, i64, i32, dbl, P, P, P, P, i64, P, P, P, P, i32]
+        L.oracle_user_loss_rows.restype = dbl
         L.oracle_max_threads.restype = i32
         _lib = L
     return _lib
@@ -129,3 +131,23 @@ def user_loss(m, n, f, lam, csr, Y, held, threads=0) -> float:
     hr, hc, hv = (_c(held[0], np.int32), _c(held[1], np.int32), _c(held[2], np.float32))
     return float(lib().oracle_user_loss(m, n, f, lam, _p(cp), _p(ci), _p(cv), _p(Y), len(hv),
                                         _p(hr), _p(hc), _p(hv), threads))
+
+
+def user_loss_rows(m, n, f, lam, csr, Y, held, row_mask, threads=0) -> float:
+    """Held-out loss of the FP64 user half-sweep restricted to the rows in row_mask."""
+    cp, ci, cv = (_c(csr[0], np.int32), _c(csr[1], np.int32), _c(csr[2], np.float32))
+    Y = _c(Y, np.float64)
+    hr, hc, hv = (_c(held[0], np.int32), _c(held[1], np.int32), _c(held[2], np.float32))
+    mask = _c(row_mask, np.uint8)
+    return float(lib().oracle_user_loss_rows(m, n, f, lam, _p(cp), _p(ci), _p(cv), _p(Y), len(hv),
+                                             _p(hr), _p(hc), _p(hv), _p(mask), threads))
+
+
+def rows_touching(m, csr, held, item):
+    """Rows whose training ratings or held-out ratings involve `item`."""
+    ptr, idx = np.asarray(csr[0]), np.asarray(csr[1])
+    rows = np.repeat(np.arange(m, dtype=np.int64), np.diff(ptr))
+    mask = np.zeros(m, np.uint8)
+    mask[rows[idx == item]] = 1
+    mask[np.asarray(held[0])[np.asarray(held[1]) == item]] = 1
+    return mask

@@ -149,3 +149,30 @@ def test_adjoint_matches_central_differences():
         assert G[i, k] == pytest.approx(fd, rel=1e-5, abs=1e-8), (i, k)
     fd = (O.user_loss(m, n, f, lam + h, csr, Y, held) - O.user_loss(m, n, f, lam - h, csr, Y, held)) / (2 * h)
     assert dlam == pytest.approx(fd, rel=1e-5)
+
+
+def test_adjoint_central_differences_on_workload5_shape():
+    """64 random coordinates of dL/dY and dL/dlambda on a scaled MovieLens-latest-shaped workload
+    (f = 128), FP64 central differences of the loss restricted to the rows each item touches."""
+    import cuda_als_gb300 as ca
+
+    tr, te, info = ca.synth_generate(5, scale=0.03)
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    csr = (tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, tr.h_csr_coo_vals)
+    held = (te.h_coo_row_idxs, te.h_csr_coo_col_idxs, te.h_csr_coo_vals)
+    rng = np.random.default_rng(5)
+    Y = rng.standard_normal((n, f)) * 0.2
+    loss, X, G, dlam = O.user_adjoint(m, n, f, lam, csr, Y, held)
+    h = 1e-5
+    items = rng.integers(0, n, 64)
+    ks = rng.integers(0, f, 64)
+    for i, k in zip(items, ks):
+        mask = O.rows_touching(m, csr, held, int(i))
+        Yp, Ym = Y.copy(), Y.copy()
+        Yp[i, k] += h
+        Ym[i, k] -= h
+        fd = (O.user_loss_rows(m, n, f, lam, csr, Yp, held, mask) -
+              O.user_loss_rows(m, n, f, lam, csr, Ym, held, mask)) / (2 * h)
+        assert G[i, k] == pytest.approx(fd, rel=1e-5, abs=1e-9), (int(i), int(k))
+    fd = (O.user_loss(m, n, f, lam + h, csr, Y, held) - O.user_loss(m, n, f, lam - h, csr, Y, held)) / (2 * h)
+    assert dlam == pytest.approx(fd, rel=1e-5)
