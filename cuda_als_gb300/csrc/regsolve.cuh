@@ -93,17 +93,20 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
 }
 
 // Cholesky of the padded FP x FP matrix; thread i holds row i in a[] and leaves L[i][0..i] there.
-// Ls (FP x LS floats, LS = FP + 4) receives every row of L as it is finished.  Returns false on
-// this thread if its pivot was not positive and finite (the caller reduces the flag).
+// Ls (FP x LS floats, LS = FP + 4) receives every row of L as it is finished; Dv (FP/8 blocks of
+// 8 x 8 floats) receives the inverse of each 8 x 8 diagonal block of L, which turns the triangular
+// solves of the rows below a block, and later the block steps of the forward / backward solves,
+// into small matrix-vector products instead of 8-step dependency chains.  Returns false on this
+// thread if its pivot was not positive and finite (the caller reduces the flag).
 template <int FP>
-__device__ bool chol_reg(float (&a)[FP], int i, float *Ls, const GroupSync &gs) {
+__device__ bool chol_reg(float (&a)[FP], int i, float *Ls, float *Dv, const GroupSync &gs) {
     constexpr int LS = FP + 4;
+    constexpr int B = 8;
     const int lane = threadIdx.x & 31;
     const int wrow0 = i - lane;  // first row of this warp
     bool ok = true;
 #pragma unroll
-    for (int K = 0; K < FP / 8; ++K) {
-        constexpr int B = 8;
+    for (int K = 0; K < FP / B; ++K) {
         const int k0 = K * B;
         const bool active = wrow0 + 31 >= k0;  // some row of this warp is at or below the block
         if (active && k0 > 0) {
@@ -123,23 +126,23 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, const GroupSync &gs) 
                 a[k0 + kk] -= s0 + s1;
             }
         }
-        // the owner warp factors the diagonal block with shuffles
+        float *dv = Dv + K * B * B;  // dv[r * 8 + c] = (L_block^-1)[r][c]
         if (wrow0 <= k0 && k0 < wrow0 + 32) {
+            // the owner warp factors the diagonal block with shuffles (rsqrt, no divisions)
             const int src0 = k0 - wrow0;  // lane of row k0
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
-                // diagonal of row k0+kk
                 float d2 = a[k0 + kk];
 #pragma unroll
                 for (int q = 0; q < kk; ++q) d2 -= a[k0 + q] * a[k0 + q];
                 const float dk2 = __shfl_sync(0xffffffffu, d2, src0 + kk);
                 const bool good = dk2 > 0.f && isfinite(dk2);
-                const float dk = good ? sqrtf(dk2) : 1.f;
+                const float inv = good ? rsqrtf(dk2) : 1.f;
+                const float dk = good ? dk2 * inv : 1.f;
                 if (i == k0 + kk) {
                     a[k0 + kk] = dk;
                     ok = ok && good;
                 }
-                // rows below it inside the block
                 float lkq[B];
 #pragma unroll
                 for (int q = 0; q < kk; ++q) lkq[q] = __shfl_sync(0xffffffffu, a[k0 + q], src0 + kk);
@@ -147,26 +150,46 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, const GroupSync &gs) 
                     float s = a[k0 + kk];
 #pragma unroll
                     for (int q = 0; q < kk; ++q) s -= a[k0 + q] * lkq[q];
-                    a[k0 + kk] = s / dk;
+                    a[k0 + kk] = s * inv;
                 }
             }
             if (i >= k0 && i < k0 + B) {  // publish the block's rows (columns 0..k0+7)
                 float *li = Ls + i * LS;
 #pragma unroll
                 for (int q = 0; q < k0 + B; q += 4)
-                    *reinterpret_cast<float4 *>(li + q) = make_float4(a[q], a[q + 1], a[q + 2], a[q + 3]);
+                    *reinterpret_cast<float4 *>(li + q) =
+                        make_float4(a[q], a[q + 1], a[q + 2], a[q + 3]);
+            }
+            __syncwarp();
+            if (i >= k0 && i < k0 + B) {
+                // column c = i - k0 of the block inverse: d_c = 1 / L_cc,
+                // d_r = -(sum_{c <= t < r} L_rt d_t) / L_rr for r > c
+                const int c = i - k0;
+                const float *lb = Ls + k0 * LS + k0;  // lb[r * LS + t] = L[k0+r][k0+t]
+                float d[B];
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    float acc = r == c ? 1.f : 0.f;
+#pragma unroll
+                    for (int t = 0; t < r; ++t)
+                        if (t >= c) acc -= lb[r * LS + t] * d[t];
+                    d[r] = r >= c ? acc / lb[r * LS + r] : 0.f;
+                    dv[r * B + c] = d[r];
+                }
             }
         }
         gs.sync();
-        // rows below the block: the 8 x 8 triangular solve against the published block rows
+        // rows below the block: L[i][block] = s L_block^-T, s = the block columns after (a)
         if (active && i >= k0 + B && i < FP) {
+            float sblk[B];
+#pragma unroll
+            for (int q = 0; q < B; ++q) sblk[q] = a[k0 + q];
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
-                const float *lk = Ls + (k0 + kk) * LS;
-                float s = a[k0 + kk];
+                float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q < kk; ++q) s -= a[k0 + q] * lk[k0 + q];
-                a[k0 + kk] = s / lk[k0 + kk];
+                for (int q = 0; q <= kk; ++q) acc = fmaf(sblk[q], dv[kk * B + q], acc);
+                a[k0 + kk] = acc;
             }
             float *li = Ls + i * LS + k0;
             *reinterpret_cast<float4 *>(li) = make_float4(a[k0], a[k0 + 1], a[k0 + 2], a[k0 + 3]);
@@ -178,29 +201,35 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, const GroupSync &gs) 
     return ok;
 }
 
-// x = (L L^T)^-1 b with L in Ls (rows) and in each thread's registers; thread i returns x_i.
-// yv (FP floats) is shared scratch.
+// x = (L L^T)^-1 b with L in Ls (rows), in each thread's registers, and the diagonal-block
+// inverses in Dv; thread i returns x_i.  yv (FP floats) is shared scratch.
 template <int FP>
 __device__ float chol_solve_reg(const float (&a)[FP], float bi, int i, const float *Ls,
-                                float *yv, const GroupSync &gs) {
+                                const float *Dv, float *yv, const GroupSync &gs) {
     constexpr int LS = FP + 4;
     constexpr int B = 8;
     const int lane = threadIdx.x & 31;
     const int wrow0 = i - lane;
-    // forward: y_i = (b_i - sum_{j<i} L_ij y_j) / L_ii, in blocks of 8 rows
+    // forward: y_block = L_block^-1 (b_block - sum over earlier blocks), one block at a time
     float acc = bi;
 #pragma unroll
     for (int K = 0; K < FP / B; ++K) {
         const int k0 = K * B;
+        const float *dv = Dv + K * B * B;
         if (wrow0 <= k0 && k0 < wrow0 + 32) {
             const int src0 = k0 - wrow0;
+            float r[B];
 #pragma unroll
-            for (int kk = 0; kk < B; ++kk) {
-                const float yk = __shfl_sync(0xffffffffu, acc / a[k0 + kk], src0 + kk);
-                if (i == k0 + kk) acc = yk;
-                if (i > k0 + kk && i < k0 + B) acc -= a[k0 + kk] * yk;
+            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, acc, src0 + q);
+            if (i >= k0 && i < k0 + B) {
+                const int c = i - k0;
+                float y = 0.f;
+#pragma unroll
+                for (int q = 0; q < B; ++q)
+                    if (q <= c) y = fmaf(dv[c * B + q], r[q], y);
+                acc = y;
+                yv[i] = y;
             }
-            if (i >= k0 && i < k0 + B) yv[i] = acc;
         }
         gs.sync();
         if (i >= k0 + B) {
@@ -209,21 +238,26 @@ __device__ float chol_solve_reg(const float (&a)[FP], float bi, int i, const flo
         }
     }
     gs.sync();
-    // backward: x_i = (y_i - sum_{j>i} L_ji x_j) / L_ii, blocks from the bottom
+    // backward: x_block = L_block^-T (y_block - sum over later blocks), blocks from the bottom
     float x = i < FP ? yv[i] : 0.f;
 #pragma unroll
     for (int K = FP / B - 1; K >= 0; --K) {
         const int k0 = K * B;
+        const float *dv = Dv + K * B * B;
         if (wrow0 <= k0 && k0 < wrow0 + 32) {
             const int src0 = k0 - wrow0;
+            float r[B];
 #pragma unroll
-            for (int kk = B - 1; kk >= 0; --kk) {
-                const int k = k0 + kk;
-                const float xk = __shfl_sync(0xffffffffu, x / Ls[k * LS + k], src0 + kk);
-                if (i == k) x = xk;
-                if (i >= k0 && i < k) x -= Ls[k * LS + i] * xk;
+            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, x, src0 + q);
+            if (i >= k0 && i < k0 + B) {
+                const int c = i - k0;
+                float xs = 0.f;
+#pragma unroll
+                for (int q = 0; q < B; ++q)
+                    if (q >= c) xs = fmaf(dv[q * B + c], r[q], xs);
+                x = xs;
+                yv[i] = xs;
             }
-            if (i >= k0 && i < k0 + B) yv[i] = x;
         }
         gs.sync();
         if (i < k0) {

@@ -57,7 +57,8 @@ struct GroupSmem {
 };
 template <int FP, int SOLVER>
 struct GroupLayout {
-    static constexpr size_t ls_floats = SOLVER == 0 ? 0 : GroupSmem<FP>::ls_floats;
+    // Cholesky / LU: L rows (or the Gram) then the 8 x 8 diagonal-block inverses
+    static constexpr size_t ls_floats = SOLVER == 0 ? 0 : GroupSmem<FP>::ls_floats + 8 * FP;
     static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
@@ -75,7 +76,7 @@ inline int fp_of(int f) {
 
 inline size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
-    return solver == 0 ? vec : (size_t)fp * (fp + 4) + vec;
+    return solver == 0 ? vec : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
 }
 
 inline Geometry geometry(int f, int solver) {
@@ -287,11 +288,12 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         gs.sync();
     } else {
         // Cholesky (+ refinement against the TMEM copy of A)
-        good = chol_reg<FP>(a, i, Ls, gs);
+        float *Dv = Ls + GroupSmem<FP>::ls_floats;
+        good = chol_reg<FP>(a, i, Ls, Dv, gs);
         const float bad = gsum128(good ? 0.f : 1.f, red, slot, gs);
         good = bad == 0.f;
         if (good) {
-            xi = chol_solve_reg<FP>(a, bi, i, Ls, yv, gs);
+            xi = chol_solve_reg<FP>(a, bi, i, Ls, Dv, yv, gs);
             // condition estimate from the Cholesky diagonal: (max L_ii / min L_ii)^2
             float lii = 1.f;
 #pragma unroll
@@ -311,7 +313,7 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                 else
                     ri = bi - (float)ax - reg * xi;
                 if (i >= f) ri = 0.f;
-                const float di = chol_solve_reg<FP>(a, ri, i, Ls, yv, gs);
+                const float di = chol_solve_reg<FP>(a, ri, i, Ls, Dv, yv, gs);
                 xi += di;
             }
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
