@@ -151,6 +151,11 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Arrive on `bar` once every cp.async this thread issued so far has landed (pending count is not
+// raised: the arrival counts against the barrier's expected count).
+__device__ __forceinline__ void cp_arrive_noinc(uint32_t bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
@@ -192,18 +197,29 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
         : "memory");
 }
+// TMEM -> registers.  The load and its wait::ld sit in one asm block, so the outputs are only
+// defined once the data has arrived.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     uint32_t r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-        "%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        "{\n\ttcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+    uint32_t r[32];
+    asm volatile(
+        "{\n\ttcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // ------------------------------------------------------------------------------------- kernels
@@ -243,14 +259,23 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     float *xo = p.X + (int64_t)m.row * f;
     const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
 
+    // the CG warm start is a global load: issue it before the TMEM reads so they overlap
+    const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
     float a[FP];
 #pragma unroll
-    for (int c = 0; c < FP; c += 16) {
-        if (c < p.ng) {
-            tmem_ld16(tb + c, &a[c]);
+    for (int c = 0; c < FP; c += 32) {
+        if (c + 32 <= FP && c + 32 <= p.ng) {
+            tmem_ld32(tb + c, &a[c]);
         } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) a[c + j] = 0.f;
+            for (int h = 0; h < 32 && c + h < FP; h += 16) {
+                if (c + h < p.ng) {
+                    tmem_ld16(tb + c + h, &a[c + h]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) a[c + h + j] = 0.f;
+                }
+            }
         }
     }
     float bi;
@@ -267,7 +292,7 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     float xi = 0.f;
     bool good = true;
     if constexpr (SOLVER == SOLVER_CG) {
-        xi = cg_reg<FP>(a, bi, i < f ? xo[i] : 0.f, i, sv, red, p.cg_iters, p.cg_tol, gs);
+        xi = cg_reg<FP>(a, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
     } else if constexpr (SOLVER == SOLVER_LU) {
         // reference semantics: LU without pivoting of the full matrix, in shared memory
         const int GS = gs_of(f);
@@ -331,7 +356,6 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 template <int FP, int SOLVER>
 __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER);
-    constexpr int LAG = NSTAGE - 1;  // stages of copies in flight per producer lane
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
@@ -356,7 +380,7 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
-            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&full[s]), 33);  // 32 producer lanes' copies + lane 0's arrive
             mbar_init(smem_u32(&empty[s]), 1);
         }
         for (int b = 0; b < MAX_NBUF; ++b) {
@@ -395,13 +419,16 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
         const int head = 4 * (int)gridDim.x;
         const char *ybytes = reinterpret_cast<const char *>(p.Ybf);
         uint32_t it = 0;        // stage counter
-        uint32_t pending = 0;   // stages whose copies are issued but not yet signalled
         bool ok = true;
         int grab_size = 1;
-        auto signal_oldest = [&](uint32_t stage_it) {
+        // A stage completes when every lane's copies have landed (cp.async arrive, no waiting
+        // here) and lane 0 has published its metadata and rating tile (ordinary arrive after a
+        // proxy fence, so the tensor core sees the generic stores).
+        auto signal_stage = [&](int s) {
+            cp_arrive_noinc(smem_u32(&full[s]));
             fence_async_smem();
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&full[stage_it % NSTAGE]));
+            if (lane == 0) mbar_arrive(smem_u32(&full[s]));
         };
         auto grab = [&](int &cbase, int &ccnt) {
             int b = 0;
@@ -491,7 +518,6 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
                         ++k;
                     }
                 }
-                cp_commit();
                 if (lane == 0) {
                     Meta m;
                     m.row = row;
@@ -500,12 +526,7 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
                     m.nu = end - beg;
                     smeta[s] = m;
                 }
-                ++pending;
-                if (pending > LAG) {
-                    cp_wait<LAG>();
-                    signal_oldest(it - LAG);
-                    --pending;
-                }
+                signal_stage(s);
                 ++it;
                 j = j1;
                 base = b1;
@@ -541,16 +562,12 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
                     m.nu = 0;
                     smeta[s] = m;
                 }
-                cp_commit();
-                ++pending;
+                signal_stage(s);
                 ++it;
             }
         }
-        cp_wait<0>();
-        while (pending > 0) {  // signal what is still in flight, oldest first
-            signal_oldest(it - pending);
-            --pending;
-        }
+        cp_commit();
+        cp_wait<0>();  // nothing of this warp is in flight when the CTA tears down
         if (!ok) {
             *abort = 1;
             if (lane == 0) atomicAdd(&p.flags[2], 1);
