@@ -8,11 +8,11 @@
 //
 //   cg_reg        warm-started CG of cumf_als_cg/cg.cu:37-232 (same recurrences, same exit rule
 //                 r'r < tol); the matvec reads p from shared memory as float4 broadcasts.
-//   chol_reg      Cholesky A = L L^T, left-looking in blocks of 8 columns: the bulk of the work
-//                 (dot products with the already published rows of L) runs on each thread's own
-//                 registers; the 8 x 8 diagonal block is factored by its owner warp with shuffles;
+//   chol_fac      Cholesky A = L L^T of the Gram copied to shared memory, left-looking in blocks
+//                 of 8 columns (a compact runtime loop, so the code stays in the instruction
+//                 cache); the 8 x 8 diagonal block is factored and inverted by its owner warp;
 //                 one barrier publishes it, one publishes the block column.
-//   chol_solve_reg  L y = b and L^T x = y in the same 8-row blocks.
+//   chol_solve_warp  L y = b and L^T x = y by one warp with shuffles and no barrier.
 // Sums over threads are combined in a fixed order (deterministic).
 #pragma once
 
@@ -92,73 +92,101 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
     return xi;
 }
 
-// Cholesky of the padded FP x FP matrix; thread i holds row i in a[] and leaves L[i][0..i] there.
-// Ls (FP x LS floats, LS = FP + 4) receives every row of L as it is finished; Dv (FP/8 blocks of
-// 8 x 8 floats) receives the inverse of each 8 x 8 diagonal block of L, which turns the triangular
-// solves of the rows below a block, and later the block steps of the forward / backward solves,
-// into small matrix-vector products instead of 8-step dependency chains.  Returns false on this
-// thread if its pivot was not positive and finite (the caller reduces the flag).
+// Cholesky of the padded FP x FP matrix held in shared memory.  On entry row i of A sits in
+// Ls[i * LS .. i * LS + FP) (LS = FP + 4; every row written and published by a barrier); on exit
+// Ls[i * LS + j] = L[i][j] for j <= i (the entries right of the diagonal are left as they were),
+// Dv holds the inverse of each 8 x 8 diagonal block of L (Dv[K * 64 + r * 8 + c] =
+// (L_KK^-1)[r][c]) and invd[j] = 1 / L[j][j].
+//
+// Left-looking in blocks of 8 columns.  Step (a) subtracts the products with the finished rows of
+// L: a runtime loop over 8-column chunks, the thread's own row read as two float4 (rows are LS
+// floats apart, so a quarter warp's float4 loads hit distinct banks) and the 8 block rows as
+// float4 broadcasts.  The owner warp factors the diagonal block with shuffles (rsqrt pivots) and
+// inverts it; the rows below then take their block columns as s L_KK^-T.  Two barriers per block.
+// Returns false on a thread whose pivot was not positive and finite.
 template <int FP>
-__device__ bool chol_reg(float (&a)[FP], int i, float *Ls, float *Dv, const GroupSync &gs) {
+__device__ bool chol_fac(int i, float *Ls, float *Dv, float *invd, const GroupSync &gs) {
     constexpr int LS = FP + 4;
     constexpr int B = 8;
     const int lane = threadIdx.x & 31;
     const int wrow0 = i - lane;  // first row of this warp
+    const bool live = i < FP;
+    float *li = Ls + (live ? i : 0) * LS;
     bool ok = true;
-#pragma unroll
+#pragma unroll 1
     for (int K = 0; K < FP / B; ++K) {
         const int k0 = K * B;
-        const bool active = wrow0 + 31 >= k0;  // some row of this warp is at or below the block
-        if (active && k0 > 0) {
-            // a[k] -= sum_{p<k0} L[i][p] L[k][p] for the 8 columns k of the block
+        float blk[B];
 #pragma unroll
-            for (int kk = 0; kk < B; ++kk) {
-                const float *lk = Ls + (k0 + kk) * LS;
-                float s0 = 0.f, s1 = 0.f;
+        for (int q = 0; q < B; ++q) blk[q] = 0.f;
+        if (live && i >= k0) {
+            const float4 t0 = *reinterpret_cast<const float4 *>(li + k0);
+            const float4 t1 = *reinterpret_cast<const float4 *>(li + k0 + 4);
+            float s[B];
 #pragma unroll
-                for (int q = 0; q < k0; q += 4) {
-                    const float4 l = *reinterpret_cast<const float4 *>(lk + q);
-                    s0 = fmaf(a[q], l.x, s0);
-                    s1 = fmaf(a[q + 1], l.y, s1);
-                    s0 = fmaf(a[q + 2], l.z, s0);
-                    s1 = fmaf(a[q + 3], l.w, s1);
+            for (int q = 0; q < B; ++q) s[q] = 0.f;
+#pragma unroll 2
+            for (int q = 0; q < k0; q += 8) {
+                const float4 o0 = *reinterpret_cast<const float4 *>(li + q);
+                const float4 o1 = *reinterpret_cast<const float4 *>(li + q + 4);
+#pragma unroll
+                for (int kk = 0; kk < B; ++kk) {
+                    const float *lk = Ls + (k0 + kk) * LS + q;
+                    const float4 l0 = *reinterpret_cast<const float4 *>(lk);
+                    const float4 l1 = *reinterpret_cast<const float4 *>(lk + 4);
+                    float t = s[kk];
+                    t = fmaf(o0.x, l0.x, t);
+                    t = fmaf(o0.y, l0.y, t);
+                    t = fmaf(o0.z, l0.z, t);
+                    t = fmaf(o0.w, l0.w, t);
+                    t = fmaf(o1.x, l1.x, t);
+                    t = fmaf(o1.y, l1.y, t);
+                    t = fmaf(o1.z, l1.z, t);
+                    t = fmaf(o1.w, l1.w, t);
+                    s[kk] = t;
                 }
-                a[k0 + kk] -= s0 + s1;
             }
+            blk[0] = t0.x - s[0];
+            blk[1] = t0.y - s[1];
+            blk[2] = t0.z - s[2];
+            blk[3] = t0.w - s[3];
+            blk[4] = t1.x - s[4];
+            blk[5] = t1.y - s[5];
+            blk[6] = t1.z - s[6];
+            blk[7] = t1.w - s[7];
         }
-        float *dv = Dv + K * B * B;  // dv[r * 8 + c] = (L_block^-1)[r][c]
+        float *dv = Dv + K * B * B;
         if (wrow0 <= k0 && k0 < wrow0 + 32) {
             // the owner warp factors the diagonal block with shuffles (rsqrt, no divisions)
             const int src0 = k0 - wrow0;  // lane of row k0
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
-                float d2 = a[k0 + kk];
+                float d2 = blk[kk];
 #pragma unroll
-                for (int q = 0; q < kk; ++q) d2 -= a[k0 + q] * a[k0 + q];
+                for (int q = 0; q < kk; ++q) d2 -= blk[q] * blk[q];
                 const float dk2 = __shfl_sync(0xffffffffu, d2, src0 + kk);
                 const bool good = dk2 > 0.f && isfinite(dk2);
                 const float inv = good ? rsqrtf(dk2) : 1.f;
                 const float dk = good ? dk2 * inv : 1.f;
                 if (i == k0 + kk) {
-                    a[k0 + kk] = dk;
+                    blk[kk] = dk;
+                    invd[i] = inv;
                     ok = ok && good;
                 }
                 float lkq[B];
 #pragma unroll
-                for (int q = 0; q < kk; ++q) lkq[q] = __shfl_sync(0xffffffffu, a[k0 + q], src0 + kk);
+                for (int q = 0; q < kk; ++q) lkq[q] = __shfl_sync(0xffffffffu, blk[q], src0 + kk);
                 if (i > k0 + kk && i < k0 + B) {
-                    float s = a[k0 + kk];
+                    float s = blk[kk];
 #pragma unroll
-                    for (int q = 0; q < kk; ++q) s -= a[k0 + q] * lkq[q];
-                    a[k0 + kk] = s * inv;
+                    for (int q = 0; q < kk; ++q) s -= blk[q] * lkq[q];
+                    blk[kk] = s * inv;
                 }
             }
-            if (i >= k0 && i < k0 + B) {  // publish the block's rows (columns 0..k0+7)
-                float *li = Ls + i * LS;
-#pragma unroll
-                for (int q = 0; q < k0 + B; q += 4)
-                    *reinterpret_cast<float4 *>(li + q) =
-                        make_float4(a[q], a[q + 1], a[q + 2], a[q + 3]);
+            if (i >= k0 && i < k0 + B) {  // publish the block's part of the row
+                *reinterpret_cast<float4 *>(li + k0) = make_float4(blk[0], blk[1], blk[2], blk[3]);
+                *reinterpret_cast<float4 *>(li + k0 + 4) =
+                    make_float4(blk[4], blk[5], blk[6], blk[7]);
             }
             __syncwarp();
             if (i >= k0 && i < k0 + B) {
@@ -166,6 +194,7 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, float *Dv, const Grou
                 // d_r = -(sum_{c <= t < r} L_rt d_t) / L_rr for r > c
                 const int c = i - k0;
                 const float *lb = Ls + k0 * LS + k0;  // lb[r * LS + t] = L[k0+r][k0+t]
+                const float *ib = invd + k0;
                 float d[B];
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
@@ -173,100 +202,133 @@ __device__ bool chol_reg(float (&a)[FP], int i, float *Ls, float *Dv, const Grou
 #pragma unroll
                     for (int t = 0; t < r; ++t)
                         if (t >= c) acc -= lb[r * LS + t] * d[t];
-                    d[r] = r >= c ? acc / lb[r * LS + r] : 0.f;
+                    d[r] = r >= c ? acc * ib[r] : 0.f;
                     dv[r * B + c] = d[r];
                 }
             }
         }
         gs.sync();
         // rows below the block: L[i][block] = s L_block^-T, s = the block columns after (a)
-        if (active && i >= k0 + B && i < FP) {
-            float sblk[B];
-#pragma unroll
-            for (int q = 0; q < B; ++q) sblk[q] = a[k0 + q];
+        if (live && i >= k0 + B) {
+            float o[B];
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
                 float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q <= kk; ++q) acc = fmaf(sblk[q], dv[kk * B + q], acc);
-                a[k0 + kk] = acc;
+                for (int q = 0; q <= kk; ++q) acc = fmaf(blk[q], dv[kk * B + q], acc);
+                o[kk] = acc;
             }
-            float *li = Ls + i * LS + k0;
-            *reinterpret_cast<float4 *>(li) = make_float4(a[k0], a[k0 + 1], a[k0 + 2], a[k0 + 3]);
-            *reinterpret_cast<float4 *>(li + 4) =
-                make_float4(a[k0 + 4], a[k0 + 5], a[k0 + 6], a[k0 + 7]);
+            *reinterpret_cast<float4 *>(li + k0) = make_float4(o[0], o[1], o[2], o[3]);
+            *reinterpret_cast<float4 *>(li + k0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
         }
         gs.sync();
     }
     return ok;
 }
 
-// x = (L L^T)^-1 b with L in Ls (rows), in each thread's registers, and the diagonal-block
-// inverses in Dv; thread i returns x_i.  yv (FP floats) is shared scratch.
+// x = (L L^T)^-1 v for the factor left by chol_fac, run by ONE warp (lane = its lane) with no
+// barrier: lane l keeps the running values of rows l, l + 32, l + 64, l + 96 in registers.  Each
+// 8-row block is a shuffle of its rows' values, a product with the block inverse (every lane
+// computes all 8 results, so nothing is broadcast), and an update of the rows after it (forward)
+// or before it (backward).  v (FP floats of shared memory) holds b on entry and x on exit.
 template <int FP>
-__device__ float chol_solve_reg(const float (&a)[FP], float bi, int i, const float *Ls,
-                                const float *Dv, float *yv, const GroupSync &gs) {
+__device__ __forceinline__ float pick(const float (&v)[(FP + 31) / 32], int j) {
+    float r = v[0];
+#pragma unroll
+    for (int q = 1; q < (FP + 31) / 32; ++q)
+        if (j == q) r = v[q];
+    return r;
+}
+
+template <int FP>
+__device__ void chol_solve_warp(int lane, const float *Ls, const float *Dv, float *v) {
     constexpr int LS = FP + 4;
     constexpr int B = 8;
-    const int lane = threadIdx.x & 31;
-    const int wrow0 = i - lane;
-    // forward: y_block = L_block^-1 (b_block - sum over earlier blocks), one block at a time
-    float acc = bi;
+    constexpr int NJ = (FP + 31) / 32;
+    float acc[NJ];
 #pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const int r = lane + 32 * j;
+        acc[j] = r < FP ? v[r] : 0.f;
+    }
+    // forward: L y = b.  The block loops stay rolled (compact code, no hoisted loads); the
+    // running value of the block's rows is picked from acc[] by selects, not by indexing.
+#pragma unroll 1
     for (int K = 0; K < FP / B; ++K) {
-        const int k0 = K * B;
+        const int k0 = K * B, jb = k0 >> 5, l0 = k0 & 31;
         const float *dv = Dv + K * B * B;
-        if (wrow0 <= k0 && k0 < wrow0 + 32) {
-            const int src0 = k0 - wrow0;
-            float r[B];
+        const float cur = pick<FP>(acc, jb);
+        float r[B], y[B];
 #pragma unroll
-            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, acc, src0 + q);
-            if (i >= k0 && i < k0 + B) {
-                const int c = i - k0;
-                float y = 0.f;
+        for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, cur, l0 + q);
+        float mine = cur;
 #pragma unroll
-                for (int q = 0; q < B; ++q)
-                    if (q <= c) y = fmaf(dv[c * B + q], r[q], y);
-                acc = y;
-                yv[i] = y;
+        for (int c = 0; c < B; ++c) {
+            float t = 0.f;
+#pragma unroll
+            for (int q = 0; q <= c; ++q) t = fmaf(dv[c * B + q], r[q], t);
+            y[c] = t;
+            if (lane == l0 + c) mine = t;
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int row = lane + 32 * j;
+            if (j == jb) {
+                if (row >= k0 && row < k0 + B) acc[j] = mine;
+            }
+            if (row >= k0 + B && row < FP) {
+                const float4 a0 = *reinterpret_cast<const float4 *>(Ls + row * LS + k0);
+                const float4 a1 = *reinterpret_cast<const float4 *>(Ls + row * LS + k0 + 4);
+                float t = acc[j];
+                t = fmaf(-a0.x, y[0], t);
+                t = fmaf(-a0.y, y[1], t);
+                t = fmaf(-a0.z, y[2], t);
+                t = fmaf(-a0.w, y[3], t);
+                t = fmaf(-a1.x, y[4], t);
+                t = fmaf(-a1.y, y[5], t);
+                t = fmaf(-a1.z, y[6], t);
+                t = fmaf(-a1.w, y[7], t);
+                acc[j] = t;
             }
         }
-        gs.sync();
-        if (i >= k0 + B) {
-#pragma unroll
-            for (int kk = 0; kk < B; ++kk) acc -= a[k0 + kk] * yv[k0 + kk];
-        }
     }
-    gs.sync();
-    // backward: x_block = L_block^-T (y_block - sum over later blocks), blocks from the bottom
-    float x = i < FP ? yv[i] : 0.f;
-#pragma unroll
+    // backward: L^T x = y, blocks from the bottom
+#pragma unroll 1
     for (int K = FP / B - 1; K >= 0; --K) {
-        const int k0 = K * B;
+        const int k0 = K * B, jb = k0 >> 5, l0 = k0 & 31;
         const float *dv = Dv + K * B * B;
-        if (wrow0 <= k0 && k0 < wrow0 + 32) {
-            const int src0 = k0 - wrow0;
-            float r[B];
+        const float cur = pick<FP>(acc, jb);
+        float r[B], x[B];
 #pragma unroll
-            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, x, src0 + q);
-            if (i >= k0 && i < k0 + B) {
-                const int c = i - k0;
-                float xs = 0.f;
+        for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, cur, l0 + q);
+        float mine = cur;
 #pragma unroll
-                for (int q = 0; q < B; ++q)
-                    if (q >= c) xs = fmaf(dv[q * B + c], r[q], xs);
-                x = xs;
-                yv[i] = xs;
+        for (int c = 0; c < B; ++c) {
+            float t = 0.f;
+#pragma unroll
+            for (int q = c; q < B; ++q) t = fmaf(dv[q * B + c], r[q], t);
+            x[c] = t;
+            if (lane == l0 + c) mine = t;
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int row = lane + 32 * j;
+            if (j == jb) {
+                if (row >= k0 && row < k0 + B) acc[j] = mine;
+            }
+            if (row < k0) {
+                float t = acc[j];
+#pragma unroll
+                for (int kk = 0; kk < B; ++kk) t = fmaf(-Ls[(k0 + kk) * LS + row], x[kk], t);
+                acc[j] = t;
             }
         }
-        gs.sync();
-        if (i < k0) {
-#pragma unroll
-            for (int kk = 0; kk < B; ++kk) x -= Ls[(k0 + kk) * LS + i] * yv[k0 + kk];
-        }
     }
-    gs.sync();
-    return x;
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+        const int r = lane + 32 * j;
+        if (r < FP) v[r] = acc[j];
+    }
 }
 
 }  // namespace als

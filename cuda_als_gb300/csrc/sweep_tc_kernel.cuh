@@ -246,6 +246,8 @@ __device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *
     return WIDE ? acc : (double)accf;
 }
 
+__device__ __forceinline__ int lane_of(int i) { return i & 31; }
+
 // The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
 template <int FP, int SOLVER>
 __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
@@ -312,23 +314,46 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         xi = i < f ? vb[i] : 0.f;
         gs.sync();
     } else {
-        // Cholesky (+ refinement against the TMEM copy of A)
+        // Cholesky (+ refinement against the TMEM copy of A).  The regularised Gram moves to
+        // shared memory, the group factors it, one warp runs each pair of triangular solves.
         float *Dv = Ls + GroupSmem<FP>::ls_floats;
-        good = chol_reg<FP>(a, i, Ls, Dv, gs);
-        const float bad = gsum128(good ? 0.f : 1.f, red, slot, gs);
-        good = bad == 0.f;
-        if (good) {
-            xi = chol_solve_reg<FP>(a, bi, i, Ls, Dv, yv, gs);
-            // condition estimate from the Cholesky diagonal: (max L_ii / min L_ii)^2
-            float lii = 1.f;
+        float *invd = vec;                                     // 1 / L_jj
+        volatile int *cflag = reinterpret_cast<volatile int *>(vec + 128);  // [0] bad, [1] wide
+        const int wg = i >> 5;                                 // warp inside the group
+        if (i < FP) {
+            float *li = Ls + i * (FP + 4);
 #pragma unroll
-            for (int j = 0; j < FP; ++j)
-                if (j == i) lii = a[j];
-            const float dmax = gmax128(i < f ? lii : 0.f, red, slot, gs);
-            const float dmin = -gmax128(i < f ? -lii : -3.0e38f, red, slot, gs);
-            const bool wide = (dmax / dmin) * (dmax / dmin) > p.cond_threshold;
+            for (int c = 0; c < FP; c += 4)
+                *reinterpret_cast<float4 *>(li + c) = make_float4(a[c], a[c + 1], a[c + 2], a[c + 3]);
+            yv[i] = bi;
+        }
+        if (et == 0) cflag[0] = 0;
+        gs.sync();
+        if (!chol_fac<FP>(i, Ls, Dv, invd, gs)) cflag[0] = 1;
+        gs.sync();
+        good = cflag[0] == 0;
+        if (good) {
+            if (wg == 0) {
+                chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
+                // condition estimate from the Cholesky diagonal: (max L_jj / min L_jj)^2
+                float dmax = 0.f, dmin = 3.0e38f;
+                for (int j = lane_of(i); j < f; j += 32) {
+                    const float l = 1.f / invd[j];
+                    dmax = fmaxf(dmax, l);
+                    dmin = fminf(dmin, l);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+                    dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+                }
+                if (i == 0) cflag[1] = (dmax / dmin) * (dmax / dmin) > p.cond_threshold ? 1 : 0;
+            }
+            gs.sync();
+            xi = i < f ? yv[i] : 0.f;
+            const bool wide = cflag[1] != 0;
             for (int s = 0; s < p.refine_steps; ++s) {
-                if (i < FP) sv[i] = i < f ? xi : 0.f;
+                if (i < FP) sv[i] = xi;
                 gs.sync();
                 const double ax = wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
                                        : tmem_rowdot<FP, false>(tb, p.ng, sv);
@@ -337,9 +362,11 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     ri = (float)((double)bi - ax - (double)reg * (double)xi);
                 else
                     ri = bi - (float)ax - reg * xi;
-                if (i >= f) ri = 0.f;
-                const float di = chol_solve_reg<FP>(a, ri, i, Ls, Dv, yv, gs);
-                xi += di;
+                if (i < FP) yv[i] = i < f ? ri : 0.f;
+                gs.sync();
+                if (wg == 0) chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
+                gs.sync();
+                if (i < f) xi += yv[i];
             }
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
         }
