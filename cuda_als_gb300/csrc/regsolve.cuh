@@ -8,10 +8,10 @@
 //
 //   cg_reg        warm-started CG of cumf_als_cg/cg.cu:37-232 (same recurrences, same exit rule
 //                 r'r < tol); the matvec reads p from shared memory as float4 broadcasts.
-//   chol_fac      Cholesky A = L L^T of the Gram copied to shared memory, left-looking in blocks
-//                 of 8 columns (a compact runtime loop, so the code stays in the instruction
-//                 cache); the 8 x 8 diagonal block is factored and inverted by its owner warp;
-//                 one barrier publishes it, one publishes the block column.
+//   chol_fac      Cholesky A = L L^T of the Gram copied to a packed lower triangle in shared
+//                 memory, left-looking in blocks of 8 columns: the dot products are spread over
+//                 all 128 threads as (row, column-half) items, one thread factors and inverts
+//                 each 8 x 8 diagonal block in registers, three barriers per block.
 //   chol_solve_warp  L y = b and L^T x = y by one warp with shuffles and no barrier.
 // Sums over threads are combined in a fixed order (deterministic).
 #pragma once
@@ -92,134 +92,144 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
     return xi;
 }
 
-// Cholesky of the padded FP x FP matrix held in shared memory.  On entry row i of A sits in
-// Ls[i * LS .. i * LS + FP) (LS = FP + 4; every row written and published by a barrier); on exit
-// Ls[i * LS + j] = L[i][j] for j <= i (the entries right of the diagonal are left as they were),
-// Dv holds the inverse of each 8 x 8 diagonal block of L (Dv[K * 64 + r * 8 + c] =
-// (L_KK^-1)[r][c]) and invd[j] = 1 / L[j][j].
-//
-// Left-looking in blocks of 8 columns.  Step (a) subtracts the products with the finished rows of
-// L: a runtime loop over 8-column chunks, the thread's own row read as two float4 (rows are LS
-// floats apart, so a quarter warp's float4 loads hit distinct banks) and the 8 block rows as
-// float4 broadcasts.  The owner warp factors the diagonal block with shuffles (rsqrt pivots) and
-// inverts it; the rows below then take their block columns as s L_KK^-T.  Two barriers per block.
-// Returns false on a thread whose pivot was not positive and finite.
+// Packed lower triangle of an FP x FP factor in shared memory.  Row i (block K = i / 8) keeps
+// columns 0 .. 8(K+1)-1, so every 8 x 8 block a row touches is whole; rows are laid out one
+// after the other with 4 floats of skew each, which keeps the float4 loads of 8 consecutive
+// rows on distinct banks.  Offsets are multiples of 4 floats (16-byte aligned float4 access).
+__device__ __forceinline__ int tri_off(int i) {
+    const int K = i >> 3;
+    return 8 * (K + 1) * (4 * K + (i & 7)) + 4 * i;
+}
 template <int FP>
-__device__ bool chol_fac(int i, float *Ls, float *Dv, float *invd, const GroupSync &gs) {
-    constexpr int LS = FP + 4;
+struct TriLayout {
+    static constexpr int floats = 32 * (FP / 8) * (FP / 8 + 1) + 4 * FP;
+};
+
+// Cholesky A = L L^T of the padded FP x FP matrix held in Ls (packed, tri_off rows; entry (i, j)
+// for j <= i must be set, the rest of each row's blocks is scratch).  On exit entry (i, j <= i)
+// holds L[i][j], Dv[K * 64 + r * 8 + c] = (L_KK^-1)[r][c] for r >= c (the inverse of each 8 x 8
+// diagonal block) and invd[j] = 1 / L[j][j].  Called by the 128 threads of a group (et = 0..127).
+//
+// Left-looking in blocks of 8 columns, three barriers per block:
+//  (a) every (row r >= k0, half h) pair subtracts L[r][0:k0] . L[k0+4h+kk][0:k0], kk < 4, from
+//      its 4 entries: work spread evenly over the 128 threads whatever the row count left;
+//  (b) one thread factors the 8 x 8 diagonal block in registers (rsqrt pivots) and inverts it;
+//  (c) every row below takes its block columns as s L_KK^-T.
+// Returns false (on thread 0) if a pivot was not positive and finite.
+template <int FP>
+__device__ bool chol_fac(int et, float *Ls, float *Dv, float *invd, const GroupSync &gs) {
     constexpr int B = 8;
-    const int lane = threadIdx.x & 31;
-    const int wrow0 = i - lane;  // first row of this warp
-    const bool live = i < FP;
-    float *li = Ls + (live ? i : 0) * LS;
     bool ok = true;
 #pragma unroll 1
     for (int K = 0; K < FP / B; ++K) {
         const int k0 = K * B;
-        float blk[B];
-#pragma unroll
-        for (int q = 0; q < B; ++q) blk[q] = 0.f;
-        if (live && i >= k0) {
-            const float4 t0 = *reinterpret_cast<const float4 *>(li + k0);
-            const float4 t1 = *reinterpret_cast<const float4 *>(li + k0 + 4);
-            float s[B];
-#pragma unroll
-            for (int q = 0; q < B; ++q) s[q] = 0.f;
+        if (k0 > 0) {
+            const int nitems = 2 * (FP - k0);
+            for (int t = et; t < nitems; t += 128) {
+                const int r = k0 + (t >> 1), c0 = k0 + 4 * (t & 1);
+                float *lr = Ls + tri_off(r);
+                const float *l0 = Ls + tri_off(c0), *l1 = Ls + tri_off(c0 + 1);
+                const float *l2 = Ls + tri_off(c0 + 2), *l3 = Ls + tri_off(c0 + 3);
+                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll 2
-            for (int q = 0; q < k0; q += 8) {
-                const float4 o0 = *reinterpret_cast<const float4 *>(li + q);
-                const float4 o1 = *reinterpret_cast<const float4 *>(li + q + 4);
-#pragma unroll
-                for (int kk = 0; kk < B; ++kk) {
-                    const float *lk = Ls + (k0 + kk) * LS + q;
-                    const float4 l0 = *reinterpret_cast<const float4 *>(lk);
-                    const float4 l1 = *reinterpret_cast<const float4 *>(lk + 4);
-                    float t = s[kk];
-                    t = fmaf(o0.x, l0.x, t);
-                    t = fmaf(o0.y, l0.y, t);
-                    t = fmaf(o0.z, l0.z, t);
-                    t = fmaf(o0.w, l0.w, t);
-                    t = fmaf(o1.x, l1.x, t);
-                    t = fmaf(o1.y, l1.y, t);
-                    t = fmaf(o1.z, l1.z, t);
-                    t = fmaf(o1.w, l1.w, t);
-                    s[kk] = t;
+                for (int q = 0; q < k0; q += 4) {
+                    const float4 o = *reinterpret_cast<const float4 *>(lr + q);
+                    const float4 a0 = *reinterpret_cast<const float4 *>(l0 + q);
+                    const float4 a1 = *reinterpret_cast<const float4 *>(l1 + q);
+                    const float4 a2 = *reinterpret_cast<const float4 *>(l2 + q);
+                    const float4 a3 = *reinterpret_cast<const float4 *>(l3 + q);
+                    s0 = fmaf(o.x, a0.x, s0); s1 = fmaf(o.x, a1.x, s1);
+                    s2 = fmaf(o.x, a2.x, s2); s3 = fmaf(o.x, a3.x, s3);
+                    s0 = fmaf(o.y, a0.y, s0); s1 = fmaf(o.y, a1.y, s1);
+                    s2 = fmaf(o.y, a2.y, s2); s3 = fmaf(o.y, a3.y, s3);
+                    s0 = fmaf(o.z, a0.z, s0); s1 = fmaf(o.z, a1.z, s1);
+                    s2 = fmaf(o.z, a2.z, s2); s3 = fmaf(o.z, a3.z, s3);
+                    s0 = fmaf(o.w, a0.w, s0); s1 = fmaf(o.w, a1.w, s1);
+                    s2 = fmaf(o.w, a2.w, s2); s3 = fmaf(o.w, a3.w, s3);
                 }
+                float4 *d = reinterpret_cast<float4 *>(lr + c0);
+                float4 v = *d;
+                v.x -= s0; v.y -= s1; v.z -= s2; v.w -= s3;
+                *d = v;
             }
-            blk[0] = t0.x - s[0];
-            blk[1] = t0.y - s[1];
-            blk[2] = t0.z - s[2];
-            blk[3] = t0.w - s[3];
-            blk[4] = t1.x - s[4];
-            blk[5] = t1.y - s[5];
-            blk[6] = t1.z - s[6];
-            blk[7] = t1.w - s[7];
+            gs.sync();
         }
-        float *dv = Dv + K * B * B;
-        if (wrow0 <= k0 && k0 < wrow0 + 32) {
-            // the owner warp factors the diagonal block with shuffles (rsqrt, no divisions)
-            const int src0 = k0 - wrow0;  // lane of row k0
+        if (et == 0) {
+            // (b) factor: right-looking inside the block, everything in registers
+            float m[B][B];
 #pragma unroll
-            for (int kk = 0; kk < B; ++kk) {
-                float d2 = blk[kk];
+            for (int r = 0; r < B; ++r) {
+                const float *lr = Ls + tri_off(k0 + r) + k0;
+                const float4 x = *reinterpret_cast<const float4 *>(lr);
+                const float4 y = *reinterpret_cast<const float4 *>(lr + 4);
+                m[r][0] = x.x; m[r][1] = x.y; m[r][2] = x.z; m[r][3] = x.w;
+                m[r][4] = y.x; m[r][5] = y.y; m[r][6] = y.z; m[r][7] = y.w;
+            }
+            float iv[B];
 #pragma unroll
-                for (int q = 0; q < kk; ++q) d2 -= blk[q] * blk[q];
-                const float dk2 = __shfl_sync(0xffffffffu, d2, src0 + kk);
+            for (int k = 0; k < B; ++k) {
+                const float dk2 = m[k][k];
                 const bool good = dk2 > 0.f && isfinite(dk2);
+                ok = ok && good;
                 const float inv = good ? rsqrtf(dk2) : 1.f;
-                const float dk = good ? dk2 * inv : 1.f;
-                if (i == k0 + kk) {
-                    blk[kk] = dk;
-                    invd[i] = inv;
-                    ok = ok && good;
-                }
-                float lkq[B];
+                m[k][k] = good ? dk2 * inv : 1.f;
+                iv[k] = inv;
 #pragma unroll
-                for (int q = 0; q < kk; ++q) lkq[q] = __shfl_sync(0xffffffffu, blk[q], src0 + kk);
-                if (i > k0 + kk && i < k0 + B) {
-                    float s = blk[kk];
+                for (int r = k + 1; r < B; ++r) m[r][k] *= inv;
 #pragma unroll
-                    for (int q = 0; q < kk; ++q) s -= blk[q] * lkq[q];
-                    blk[kk] = s * inv;
-                }
+                for (int r = k + 1; r < B; ++r)
+#pragma unroll
+                    for (int j = k + 1; j <= r; ++j) m[r][j] = fmaf(-m[r][k], m[j][k], m[r][j]);
             }
-            if (i >= k0 && i < k0 + B) {  // publish the block's part of the row
-                *reinterpret_cast<float4 *>(li + k0) = make_float4(blk[0], blk[1], blk[2], blk[3]);
-                *reinterpret_cast<float4 *>(li + k0 + 4) =
-                    make_float4(blk[4], blk[5], blk[6], blk[7]);
+#pragma unroll
+            for (int r = 0; r < B; ++r) {  // L rows (entries right of the diagonal: zero)
+                float *lr = Ls + tri_off(k0 + r) + k0;
+                *reinterpret_cast<float4 *>(lr) = make_float4(
+                    m[r][0], r >= 1 ? m[r][1] : 0.f, r >= 2 ? m[r][2] : 0.f, r >= 3 ? m[r][3] : 0.f);
+                *reinterpret_cast<float4 *>(lr + 4) =
+                    make_float4(r >= 4 ? m[r][4] : 0.f, r >= 5 ? m[r][5] : 0.f,
+                                r >= 6 ? m[r][6] : 0.f, r >= 7 ? m[r][7] : 0.f);
             }
-            __syncwarp();
-            if (i >= k0 && i < k0 + B) {
-                // column c = i - k0 of the block inverse: d_c = 1 / L_cc,
-                // d_r = -(sum_{c <= t < r} L_rt d_t) / L_rr for r > c
-                const int c = i - k0;
-                const float *lb = Ls + k0 * LS + k0;  // lb[r * LS + t] = L[k0+r][k0+t]
-                const float *ib = invd + k0;
+            *reinterpret_cast<float4 *>(invd + k0) = make_float4(iv[0], iv[1], iv[2], iv[3]);
+            *reinterpret_cast<float4 *>(invd + k0 + 4) = make_float4(iv[4], iv[5], iv[6], iv[7]);
+            // inverse, one column at a time: D[c][c] = 1 / L_cc,
+            // D[r][c] = -(sum_{c <= t < r} L[r][t] D[t][c]) / L[r][r]
+            float *dv = Dv + K * B * B;
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
                 float d[B];
 #pragma unroll
-                for (int r = 0; r < B; ++r) {
-                    float acc = r == c ? 1.f : 0.f;
+                for (int r = c; r < B; ++r) {
+                    if (r == c) {
+                        d[r] = iv[c];
+                    } else {
+                        float acc = 0.f;
 #pragma unroll
-                    for (int t = 0; t < r; ++t)
-                        if (t >= c) acc -= lb[r * LS + t] * d[t];
-                    d[r] = r >= c ? acc * ib[r] : 0.f;
+                        for (int t = c; t < r; ++t) acc = fmaf(m[r][t], d[t], acc);
+                        d[r] = -acc * iv[r];
+                    }
                     dv[r * B + c] = d[r];
                 }
             }
         }
         gs.sync();
-        // rows below the block: L[i][block] = s L_block^-T, s = the block columns after (a)
-        if (live && i >= k0 + B) {
+        // (c) rows below the block
+        const float *dv = Dv + K * B * B;
+        for (int t = et; t < FP - k0 - B; t += 128) {
+            float *lr = Ls + tri_off(k0 + B + t) + k0;
+            const float4 x = *reinterpret_cast<const float4 *>(lr);
+            const float4 y = *reinterpret_cast<const float4 *>(lr + 4);
+            const float sb[B] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
             float o[B];
 #pragma unroll
             for (int kk = 0; kk < B; ++kk) {
                 float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q <= kk; ++q) acc = fmaf(blk[q], dv[kk * B + q], acc);
+                for (int q = 0; q <= kk; ++q) acc = fmaf(sb[q], dv[kk * B + q], acc);
                 o[kk] = acc;
             }
-            *reinterpret_cast<float4 *>(li + k0) = make_float4(o[0], o[1], o[2], o[3]);
-            *reinterpret_cast<float4 *>(li + k0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
+            *reinterpret_cast<float4 *>(lr) = make_float4(o[0], o[1], o[2], o[3]);
+            *reinterpret_cast<float4 *>(lr + 4) = make_float4(o[4], o[5], o[6], o[7]);
         }
         gs.sync();
     }
@@ -242,7 +252,6 @@ __device__ __forceinline__ float pick(const float (&v)[(FP + 31) / 32], int j) {
 
 template <int FP>
 __device__ void chol_solve_warp(int lane, const float *Ls, const float *Dv, float *v) {
-    constexpr int LS = FP + 4;
     constexpr int B = 8;
     constexpr int NJ = (FP + 31) / 32;
     float acc[NJ];
@@ -277,8 +286,8 @@ __device__ void chol_solve_warp(int lane, const float *Ls, const float *Dv, floa
                 if (row >= k0 && row < k0 + B) acc[j] = mine;
             }
             if (row >= k0 + B && row < FP) {
-                const float4 a0 = *reinterpret_cast<const float4 *>(Ls + row * LS + k0);
-                const float4 a1 = *reinterpret_cast<const float4 *>(Ls + row * LS + k0 + 4);
+                const float4 a0 = *reinterpret_cast<const float4 *>(Ls + tri_off(row) + k0);
+                const float4 a1 = *reinterpret_cast<const float4 *>(Ls + tri_off(row) + k0 + 4);
                 float t = acc[j];
                 t = fmaf(-a0.x, y[0], t);
                 t = fmaf(-a0.y, y[1], t);
@@ -319,7 +328,7 @@ __device__ void chol_solve_warp(int lane, const float *Ls, const float *Dv, floa
             if (row < k0) {
                 float t = acc[j];
 #pragma unroll
-                for (int kk = 0; kk < B; ++kk) t = fmaf(-Ls[(k0 + kk) * LS + row], x[kk], t);
+                for (int kk = 0; kk < B; ++kk) t = fmaf(-Ls[tri_off(k0 + kk) + row], x[kk], t);
                 acc[j] = t;
             }
         }

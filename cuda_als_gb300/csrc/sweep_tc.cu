@@ -178,6 +178,7 @@ als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *wh
     p.ng = t->geo.ng;
     p.acc_stride = t->geo.acc_stride;
     p.tmem_cols = t->geo.tmem_cols;
+    p.nbuf = t->geo.nbuf;
     p.nepi = t->geo.nepi;
     p.solve = t->solver;
     p.cg_iters = h->cfg.cg_steps;

@@ -16,8 +16,11 @@ namespace tcg {
 constexpr int KC = 64;                       // ratings per stage
 constexpr int MAX_NSTAGE = 8;
 // Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
-// gathered bytes in flight per SM); the Cholesky / LU scratch leaves room for five stages.
-__host__ __device__ constexpr int nstage_of(int solver) { return solver == 0 ? 8 : 5; }
+// gathered bytes in flight per SM); the LU scratch leaves room for five stages, and so does the
+// Cholesky's except at FP = 112, where four factor groups share the SM.
+__host__ __device__ constexpr int nstage_of(int solver, int fp) {
+    return solver == 0 ? 8 : (solver == 1 && fp == 112) ? 4 : 5;
+}
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
@@ -42,7 +45,7 @@ struct Params {
     float *X;                  // this side's FP32 factors (in: CG warm start, out: solution)
     int32_t *work;             // atomic row counter (zeroed before the launch)
     int32_t *flags;            // [0] flagged rows, [1] FP64-refined rows, [2] timeouts
-    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, nepi, solve, cg_iters;
+    int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, nbuf, nepi, solve, cg_iters;
     int32_t refine_steps;
     float lambda, cg_tol, cond_threshold;
 };
@@ -57,8 +60,10 @@ struct GroupSmem {
 };
 template <int FP, int SOLVER>
 struct GroupLayout {
-    // Cholesky / LU: L rows (or the Gram) then the 8 x 8 diagonal-block inverses
-    static constexpr size_t ls_floats = SOLVER == 0 ? 0 : GroupSmem<FP>::ls_floats + 8 * FP;
+    // Cholesky: packed L then the 8 x 8 diagonal-block inverses; LU: the square Gram (+ unused)
+    static constexpr size_t ls_floats = SOLVER == 0   ? 0
+                                        : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
+                                                      : GroupSmem<FP>::ls_floats + 8 * FP;
     static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
@@ -76,7 +81,10 @@ inline int fp_of(int f) {
 
 inline size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
-    return solver == 0 ? vec : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
+    const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
+    return solver == 0   ? vec
+           : solver == 1 ? tri + 8 * (size_t)fp + vec
+                         : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
 }
 
 inline Geometry geometry(int f, int solver) {
@@ -87,10 +95,12 @@ inline Geometry geometry(int f, int solver) {
     const int acc_cols = g.ng + 16;
     g.acc_stride = acc_cols <= 128 ? 128 : 256;
     g.nbuf = acc_cols <= 128 ? 4 : 2;
-    g.nepi = g.nbuf / 2;
+    // CG / LU groups double-buffer their accumulator; a Cholesky group copies its Gram to shared
+    // memory at once, so it takes one buffer and twice as many groups share the SM
+    g.nepi = solver == SOLVER_CHOL ? g.nbuf : g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
     g.nthreads = 64 + 128 * g.nepi;
-    const int ns = nstage_of(solver);
+    const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
     bytes += sizeof(int32_t) * ns * KC;                              // gathered column ids
@@ -261,75 +271,55 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     float *xo = p.X + (int64_t)m.row * f;
     const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
 
-    // the CG warm start is a global load: issue it before the TMEM reads so they overlap
-    const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
-    float a[FP];
-#pragma unroll
-    for (int c = 0; c < FP; c += 32) {
-        if (c + 32 <= FP && c + 32 <= p.ng) {
-            tmem_ld32(tb + c, &a[c]);
-        } else {
-#pragma unroll
-            for (int h = 0; h < 32 && c + h < FP; h += 16) {
-                if (c + h < p.ng) {
-                    tmem_ld16(tb + c + h, &a[c + h]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) a[c + h + j] = 0.f;
-                }
-            }
-        }
-    }
     float bi;
     {
         float v[16];
         tmem_ld16(tb + p.ng, v);
         bi = i < f ? v[0] : 0.f;
     }
-#pragma unroll
-    for (int j = 0; j < FP; ++j)
-        if (j == i) a[j] = i < f ? a[j] + reg : 1.f;  // identity on the padded rows
-
     int slot = 0;
     float xi = 0.f;
     bool good = true;
-    if constexpr (SOLVER == SOLVER_CG) {
-        xi = cg_reg<FP>(a, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
-    } else if constexpr (SOLVER == SOLVER_LU) {
-        // reference semantics: LU without pivoting of the full matrix, in shared memory
-        const int GS = gs_of(f);
-        float *G = Ls;
-        if (i < f) {
-#pragma unroll
-            for (int j = 0; j < FP; ++j)
-                if (j < f) G[i * GS + j] = a[j];
-        }
-        float *vb = vec;
-        if (i < f) vb[i] = bi;
-        gs.sync();
-        if (g == 0)
-            good = lu_nopivot_solve<NamedSync<1, 128>>(G, GS, f, vb, et, 128);
-        else
-            good = lu_nopivot_solve<NamedSync<2, 128>>(G, GS, f, vb, et, 128);
-        xi = i < f ? vb[i] : 0.f;
-        gs.sync();
-    } else {
-        // Cholesky (+ refinement against the TMEM copy of A).  The regularised Gram moves to
-        // shared memory, the group factors it, one warp runs each pair of triangular solves.
-        float *Dv = Ls + GroupSmem<FP>::ls_floats;
-        float *invd = vec;                                     // 1 / L_jj
+    if constexpr (SOLVER == SOLVER_CHOL) {
+        // Cholesky (+ refinement against the TMEM copy of A).  The regularised Gram's lower
+        // triangle moves to the packed shared-memory layout in 32-column chunks (a warp reads
+        // only the chunks its rows reach), the group factors it, one warp runs each pair of
+        // triangular solves.
+        float *Dv = Ls + TriLayout<FP>::floats;
+        float *invd = vec;                                                   // 1 / L_jj
         volatile int *cflag = reinterpret_cast<volatile int *>(vec + 128);  // [0] bad, [1] wide
-        const int wg = i >> 5;                                 // warp inside the group
-        if (i < FP) {
-            float *li = Ls + i * (FP + 4);
+        const int wg = i >> 5;                                               // warp in the group
+        const int len = 8 * ((i >> 3) + 1);                                  // stored columns
+        float *li = Ls + tri_off(i < FP ? i : 0);
 #pragma unroll
-            for (int c = 0; c < FP; c += 4)
-                *reinterpret_cast<float4 *>(li + c) = make_float4(a[c], a[c + 1], a[c + 2], a[c + 3]);
-            yv[i] = bi;
+        for (int c = 0; c < FP; c += 32) {
+            if (c < 32 * (wg + 1)) {  // warp-uniform: rows 32wg.. reach column 32wg + 31
+                float v[32];
+#pragma unroll
+                for (int h = 0; h < 32; h += 16) {
+                    if (c + h < FP && c + h < p.ng) {
+                        tmem_ld16(tb + c + h, v + h);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) v[h + j] = 0.f;
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (c + j == i) v[j] = i < f ? v[j] + reg : 1.f;  // identity on padded rows
+                if (i < FP) {
+#pragma unroll
+                    for (int j = 0; j < 32 && c + j < FP; j += 4)
+                        if (c + j < len)
+                            *reinterpret_cast<float4 *>(li + c + j) =
+                                make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                }
+            }
         }
+        if (i < FP) yv[i] = bi;
         if (et == 0) cflag[0] = 0;
         gs.sync();
-        if (!chol_fac<FP>(i, Ls, Dv, invd, gs)) cflag[0] = 1;
+        if (!chol_fac<FP>(et, Ls, Dv, invd, gs)) cflag[0] = 1;
         gs.sync();
         good = cflag[0] == 0;
         if (good) {
@@ -370,6 +360,52 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             }
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
         }
+    } else {
+        // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
+        // the CG warm start is a global load: issue it before the TMEM reads so they overlap
+        const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
+        float a[FP];
+#pragma unroll
+        for (int c = 0; c < FP; c += 32) {
+            if (c + 32 <= FP && c + 32 <= p.ng) {
+                tmem_ld32(tb + c, &a[c]);
+            } else {
+#pragma unroll
+                for (int h = 0; h < 32 && c + h < FP; h += 16) {
+                    if (c + h < p.ng) {
+                        tmem_ld16(tb + c + h, &a[c + h]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) a[c + h + j] = 0.f;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < FP; ++j)
+            if (j == i) a[j] = i < f ? a[j] + reg : 1.f;  // identity on the padded rows
+
+        if constexpr (SOLVER == SOLVER_CG) {
+            xi = cg_reg<FP>(a, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
+        } else {
+            // reference semantics: LU without pivoting of the full matrix, in shared memory
+            const int GS = gs_of(f);
+            float *G = Ls;
+            if (i < f) {
+#pragma unroll
+                for (int j = 0; j < FP; ++j)
+                    if (j < f) G[i * GS + j] = a[j];
+            }
+            float *vb = vec;
+            if (i < f) vb[i] = bi;
+            gs.sync();
+            if (g == 0)
+                good = lu_nopivot_solve<NamedSync<1, 128>>(G, GS, f, vb, et, 128);
+            else
+                good = lu_nopivot_solve<NamedSync<2, 128>>(G, GS, f, vb, et, 128);
+            xi = i < f ? vb[i] : 0.f;
+            gs.sync();
+        }
     }
     const float nonfinite = gsum128((i < f && !isfinite(xi)) ? 1.f : 0.f, red, slot, gs);
     if (!good || nonfinite > 0.f) {
@@ -381,8 +417,9 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 }
 
 template <int FP, int SOLVER>
-__global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
-    constexpr int NSTAGE = nstage_of(SOLVER);
+__global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
+    sweep_tc_kernel(const Params p) {
+    constexpr int NSTAGE = nstage_of(SOLVER, FP);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
@@ -400,7 +437,7 @@ __global__ void __launch_bounds__(320, 1) sweep_tc_kernel(const Params p) {
     volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nbuf = 2 * p.nepi;
+    const int nbuf = p.nbuf;
 
     // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
     for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += blockDim.x)

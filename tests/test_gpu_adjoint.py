@@ -37,7 +37,7 @@ def test_adjoint_matches_fp64_reference(config, scale):
     loss = Fn.apply(Vt, lt)
     loss.backward()
     e_loss, X, G, e_dlam = O.user_adjoint(m, n, f, float(np.float32(lam)), csr, V, held)
-    assert float(loss) == pytest.approx(e_loss, rel=TOL_LOSS)
+    assert float(loss.detach()) == pytest.approx(e_loss, rel=TOL_LOSS)
     g = Vt.grad.numpy().astype(np.float64)
     assert np.linalg.norm(g - G) / np.linalg.norm(G) < TOL_GRAD
     assert float(lt.grad) == pytest.approx(e_dlam, rel=TOL_DLAM)
