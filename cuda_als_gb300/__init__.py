@@ -384,6 +384,15 @@ class als_model:
         return [{"lo": int(lo[i]), "kind": int(kind[i]), "solver": int(solver[i])}
                 for i in range(k)]
 
+    def tuning(self, side: int):
+        """The autotuner's per-bucket measurements (ALS_SOLVE_AUTO): CG and Cholesky ms on the
+        tuning sweep and the relative difference of their solutions; [] when nothing was tuned."""
+        nb = C.c_int32(64)
+        cg, ch, rel = (np.zeros(64, np.float32) for _ in range(3))
+        self._c(lib().als_get_tuning(self._h, side, _ptr(cg), _ptr(ch), _ptr(rel), C.byref(nb)))
+        return [{"ms_cg": float(cg[i]), "ms_cholesky": float(ch[i]), "rel_diff": float(rel[i])}
+                for i in range(nb.value)]
+
     def user_halfsweep_adjoint(self, rows, cols, vals):
         """Held-out loss of the user half-sweep, dL/dV (n x f) and dL/dlambda."""
         rows = np.ascontiguousarray(rows, np.int32)

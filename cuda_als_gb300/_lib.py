@@ -82,6 +82,7 @@ def lib() -> C.CDLL:
         "als_get_stage_ms": ([H, C.POINTER(f64)], i32),
         "als_get_counters": ([H, C.POINTER(i64)], i32),
         "als_get_plan": ([H, i32, P, P, P, C.POINTER(i32)], i32),
+        "als_get_tuning": ([H, i32, P, P, P, C.POINTER(i32)], i32),
         "als_user_halfsweep_adjoint": ([H, C.POINTER(CooView), C.POINTER(f64), P,
                                         C.POINTER(f64)], i32),
         "als_csr_to_csc": ([C.POINTER(CsrView), P, P, P], i32),
@@ -108,7 +109,7 @@ EXPORTS = [
     "als_destroy", "als_last_error", "als_set_stream", "als_update_values", "als_reload", "als_init_factors",
     "als_iterate", "als_half_sweep", "als_train", "als_rmse_test", "als_rmse_train",
     "als_get_factors", "als_set_factors", "als_get_device_factors", "als_save_libmf",
-    "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan",
+    "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan", "als_get_tuning",
     "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
     "als_csr_to_csc_device_noalloc",
     "als_degree_order", "als_synth_shape", "als_synth_generate",

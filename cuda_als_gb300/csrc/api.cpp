@@ -424,6 +424,7 @@ static als_status upload_inputs(als_handle *h, const als_csr_view *csr, const al
     H_CUDA(h, degree_order_device(m, h->d_csr_ptr, maxdeg_rows, h->d_order[0], h->d_scratch, st));
     H_CUDA(h, degree_order_device(n, h->d_csc_ptr, maxdeg_cols, h->d_order[1], h->d_scratch, st));
     H_CUDA(h, cudaStreamSynchronize(st));
+    data_changed(h);
     return tc_values_changed(h);
 }
 
@@ -558,6 +559,7 @@ extern "C" als_status als_update_values(als_handle *h, const float *vals) {
 extern "C" als_status als_init_factors(als_handle *h) {
     if (!h) return set_global_error(ALS_ERR_INVALID_ARG, "null handle");
     cudaSetDevice(h->cfg.device);
+    if (h->cfg.autotune) reset_tuning(h);  // a new run re-tunes the ALS_SOLVE_AUTO plan
     // als_model.cu:1772-1777: srand(0), VT[k] = 0.2*((float)rand()/(float)RAND_MAX), UT = 0
     std::srand(0u);
     const int64_t nf = h->n * h->f;
@@ -574,22 +576,26 @@ extern "C" als_status als_init_factors(als_handle *h) {
 extern "C" als_status als_half_sweep(als_handle *h, int32_t side) {
     if (!h || (side != 0 && side != 1)) return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
     cudaSetDevice(h->cfg.device);
-    als_status s = run_half_sweep(h, side, true);
+    H_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, h->stream));
+    als_status s = run_half_sweep(h, side);
     if (s != ALS_OK) return s;
     H_CUDA(h, cudaStreamSynchronize(h->stream));
+    s = read_stage_ms(h, side);
+    if (s != ALS_OK) return s;
     return check_sweep_flags(h);
 }
 
 extern "C" als_status als_iterate(als_handle *h, int32_t iters) {
     if (!h || iters < 0) return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
     cudaSetDevice(h->cfg.device);
-    for (int32_t it = 0; it < iters; ++it) {
-        for (int side = 0; side < 2; ++side) {
-            als_status s = run_half_sweep(h, side, it == iters - 1);
-            if (s != ALS_OK) return s;
-        }
-    }
+    H_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, h->stream));
+    als_status s = run_epochs(h, iters);
+    if (s != ALS_OK) return s;
     H_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int side = 0; side < 2 && iters > 0; ++side) {
+        s = read_stage_ms(h, side);
+        if (s != ALS_OK) return s;
+    }
     return check_sweep_flags(h);
 }
 

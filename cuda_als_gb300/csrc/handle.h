@@ -11,6 +11,15 @@
 
 struct TcState;  // tensor-core path state (sweep_tc.cu)
 
+// One nnz bucket of a side: a contiguous range of the side's descending-degree row order, run by
+// its own launch with its own solver (ALS_SOLVE_*).  The autotuner's measurements ride along.
+struct SweepBucket {
+    int32_t lo = 0, hi = 0;
+    int cls = 0;  // 0: degree >= 8f, 1: f <= degree < 8f, 2: degree < f
+    int solver = ALS_SOLVE_CHOLESKY;
+    float ms_cg = -1.f, ms_chol = -1.f, rel = -1.f;
+};
+
 struct als_handle {
     als_config cfg{};
     int precision = ALS_PREC_FP32;  // effective precision
@@ -46,6 +55,18 @@ struct als_handle {
     int64_t counters[3] = {0, 0, 0};
     std::vector<cudaEvent_t> events;
     cudaEvent_t ev_half[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    // one ALS epoch (U then V half-sweep) captured once the kernel plan is final, replayed by
+    // als_iterate; dropped whenever a pointer, the data or the plan changes
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    int64_t eager_epochs = 0;  // epochs run without a graph (capture waits for the first one)
+    // kernel plan per side: buckets (rebuilt when the ratings change), half-sweeps since the
+    // rebuild, and the autotuner's decision per degree class (kept across rating changes)
+    std::vector<SweepBucket> plan[2];
+    int sweeps[2] = {0, 0};
+    bool tuned[2] = {false, false};
+    int cls_solver[2][3] = {{ALS_SOLVE_CHOLESKY, ALS_SOLVE_CHOLESKY, ALS_SOLVE_CHOLESKY},
+                            {ALS_SOLVE_CHOLESKY, ALS_SOLVE_CHOLESKY, ALS_SOLVE_CHOLESKY}};
 
     TcState *tc = nullptr;
 
@@ -57,6 +78,10 @@ als_status prepare_precision_path(als_handle *h);
 void release_precision_path(als_handle *h);
 void invalidate_graphs(als_handle *h);
 als_status refresh_csc_values(als_handle *h);
-als_status run_half_sweep(als_handle *h, int side, bool timed);
+als_status run_half_sweep(als_handle *h, int side);
+als_status run_epochs(als_handle *h, int32_t iters);
+void data_changed(als_handle *h);
+void reset_tuning(als_handle *h);
+als_status read_stage_ms(als_handle *h, int side);
 als_status check_sweep_flags(als_handle *h);
 bool tc_supported(int f);

@@ -71,6 +71,15 @@ cudaError_t count_bad_entries(int64_t nnz, const int32_t *idx, int32_t limit, co
 // Sweep kernels
 // ---------------------------------------------------------------------------------------------
 
+// Record `ev` on `st`; while `st` is being captured into a graph the record becomes an
+// event-record node of the graph (cudaEventRecordExternal), so replays time themselves.
+inline cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
 struct SweepArgs {
     const int32_t *ptr;     // rows + 1 (this side's CSR)
     const int32_t *idx;     // nnz, indices into the opposite table
@@ -97,6 +106,9 @@ cudaError_t launch_sweep_fp32(const SweepArgs &a, cudaStream_t st, int *launches
 // ---------------------------------------------------------------------------------------------
 size_t rmse_scratch_bytes();
 // Deterministic FP64 sum of squared errors; writes the sum into *d_out (device double).
+// sum over rows order[lo..hi) of ||A_r - B_r||^2 and ||A_r||^2 (FP64) into out[0..1]
+cudaError_t launch_bucket_diff(const int32_t *order, int32_t lo, int32_t hi, const float *A,
+                               const float *B, int f, double *out, cudaStream_t st);
 cudaError_t launch_sq_error(int64_t nnz, const int32_t *rows, const int32_t *cols,
                             const float *vals, const float *U, const float *V, int f,
                             double *d_partials, double *d_out, cudaStream_t st);

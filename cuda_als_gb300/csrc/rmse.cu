@@ -8,6 +8,8 @@
 // component that is NaN (als_model.cu:78-79).  HBM/L2-bound: 12 B per rating plus two gathered
 // factor rows.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include "internal.h"
@@ -74,6 +76,53 @@ cudaError_t launch_sq_error(int64_t nnz, const int32_t *rows, const int32_t *col
     sq_error_partials_kernel<<<RMSE_BLOCKS, RMSE_THREADS, 0, st>>>(nnz, rows, cols, vals, U, V,
                                                                    f, d_partials);
     sum_partials_kernel<<<1, RMSE_THREADS, 0, st>>>(d_partials, RMSE_BLOCKS, d_out);
+    return cudaGetLastError();
+}
+
+// Relative difference of two factor tables over the rows order[lo..hi): sum (a - b)^2 and
+// sum a^2 in FP64 (the autotuner's agreement check between two solvers).
+static __global__ void bucket_diff_kernel(const int32_t *__restrict__ order, int32_t lo, int32_t hi,
+                                   const float *__restrict__ A, const float *__restrict__ Bm, int f,
+                                   double *__restrict__ out) {
+    __shared__ double sd[32], sa[32];
+    double d2 = 0.0, a2 = 0.0;
+    const int64_t total = (int64_t)(hi - lo) * f;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = order[lo + e / f];
+        const int j = (int)(e % f);
+        const double a = A[r * f + j], b = Bm[r * f + j];
+        d2 += (a - b) * (a - b);
+        a2 += a * a;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sd[threadIdx.x >> 5] = d2;
+        sa[threadIdx.x >> 5] = a2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double td = 0.0, ta = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            td += sd[w];
+            ta += sa[w];
+        }
+        atomicAdd(&out[0], td);
+        atomicAdd(&out[1], ta);
+    }
+}
+
+cudaError_t launch_bucket_diff(const int32_t *order, int32_t lo, int32_t hi, const float *A,
+                               const float *B, int f, double *out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess || hi <= lo) return e;
+    const int64_t total = (int64_t)(hi - lo) * f;
+    const int grid = (int)std::min<int64_t>((total + 255) / 256, 1216);
+    bucket_diff_kernel<<<grid, 256, 0, st>>>(order, lo, hi, A, B, f, out);
     return cudaGetLastError();
 }
 

@@ -7,7 +7,9 @@
 // is handled by fused kernels in descending-degree order with no host round trip.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <string>
+#include <vector>
 
 #include "handle.h"
 #include "internal.h"
@@ -47,7 +49,14 @@ void release_precision_path(als_handle *h) {
     tc_release(h);
 }
 
-void invalidate_graphs(als_handle *h) { tc_invalidate_graphs(h); }
+void invalidate_graphs(als_handle *h) {
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->graph_exec = nullptr;
+    h->graph = nullptr;
+    tc_invalidate_graphs(h);
+}
+
 
 als_status refresh_csc_values(als_handle *h) {
     cudaStream_t st = h->stream;
@@ -70,42 +79,247 @@ als_status refresh_csc_values(als_handle *h) {
     return tc_values_changed(h);
 }
 
-als_status run_half_sweep(als_handle *h, int side, bool timed) {
+// ---------------------------------------------------------------------------- kernel plan
+
+// Relative agreement the autotuner asks of CG against Cholesky on a bucket's rows (Frobenius norm
+// of the difference over the norm of the Cholesky solution) at the tuning sweep.
+constexpr double AUTO_TOL = 2e-2;
+
+static bool autotuned(const als_handle *h) { return h->cfg.solve_type == ALS_SOLVE_AUTO; }
+
+// Buckets of a side from the host copy of its pointer array: rows of degree >= 8f (the Gram
+// dominates), f <= degree < 8f, and degree < f (rank-deficient Gram, the solve dominates).  The
+// order array is sorted by descending degree, so each bucket is a contiguous range of it.  A fixed
+// solver makes one bucket of every row.
+static void build_plan(als_handle *h, int side) {
+    const std::vector<int32_t> &ptr = h->host_ptr[side];
+    const int64_t rows = side == 0 ? h->m : h->n;
+    std::vector<SweepBucket> &plan = h->plan[side];
+    plan.clear();
+    h->sweeps[side] = 0;
+    if (!autotuned(h) || (int64_t)ptr.size() != rows + 1) {
+        SweepBucket b;
+        b.hi = (int32_t)rows;
+        b.solver = autotuned(h) ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
+        plan.push_back(b);
+        h->tuned[side] = true;
+        return;
+    }
+    int64_t heavy = 0, mid = 0;
+    for (int64_t r = 0; r < rows; ++r) {
+        const int64_t d = ptr[r + 1] - ptr[r];
+        if (d >= 8 * (int64_t)h->f) ++heavy;
+        else if (d >= h->f) ++mid;
+    }
+    const int64_t cuts[4] = {0, heavy, heavy + mid, rows};
+    for (int k = 0; k < 3; ++k) {
+        if (cuts[k + 1] == cuts[k]) continue;
+        SweepBucket b;
+        b.lo = (int32_t)cuts[k];
+        b.hi = (int32_t)cuts[k + 1];
+        b.cls = k;
+        b.solver = h->tuned[side] ? h->cls_solver[side][k] : ALS_SOLVE_CHOLESKY;
+        plan.push_back(b);
+    }
+}
+
+// The ratings changed (creation, reload): drop the graph and the buckets; an autotuned side keeps
+// its per-class solver choice and applies it to the new buckets.
+void data_changed(als_handle *h) {
+    invalidate_graphs(h);
+    for (auto &pl : h->plan) pl.clear();
+}
+
+// Forget the autotuner's decisions (als_init_factors with autotune = 1).
+void reset_tuning(als_handle *h) {
+    if (!autotuned(h)) return;
+    invalidate_graphs(h);
+    for (int s = 0; s < 2; ++s) {
+        h->plan[s].clear();
+        h->tuned[s] = false;
+        for (int &c : h->cls_solver[s]) c = ALS_SOLVE_CHOLESKY;
+    }
+}
+
+static bool plan_final(const als_handle *h) {
+    for (int s = 0; s < 2; ++s)
+        if (h->plan[s].empty() || !h->tuned[s]) return false;
+    return true;
+}
+
+static cudaError_t launch_bucket(als_handle *h, int side, const SweepBucket &b, int solve, int slot,
+                                 int *launches) {
+    if (h->precision != ALS_PREC_FP32)
+        return tc_launch_bucket(h, side, b.lo, b.hi, solve, slot, launches);
+    SweepArgs a{};
+    a.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
+    a.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
+    a.val = side == 0 ? h->d_csr_val : h->d_csc_val;
+    a.Y = side == 0 ? h->d_V : h->d_U;
+    a.X = side == 0 ? h->d_U : h->d_V;
+    a.order = h->d_order[side];
+    a.row_begin = b.lo;
+    a.row_end = b.hi;
+    a.f = h->f;
+    a.lambda = h->cfg.lambda;
+    a.solve = solve;
+    a.cg_iters = h->cfg.cg_steps;
+    a.cg_tol = h->cfg.cg_tol;
+    a.flags = h->d_flags;
+    return launch_sweep_fp32(a, h->stream, launches);
+}
+
+// The tuning sweep of a side (ALS_SOLVE_AUTO, the side's second half-sweep: the first leaves the
+// warm start CG needs).  Every bucket runs CG and then Cholesky from the same warm start, each
+// timed with CUDA events; the bucket keeps CG where it is faster and agrees with Cholesky within
+// AUTO_TOL, Cholesky otherwise.  The factors keep the Cholesky solution and the status words
+// count the Cholesky run only.  Synchronous (the host reads the timings): never graph-captured.
+static als_status tune_side(als_handle *h, int side, int *launches) {
     cudaStream_t st = h->stream;
     const int64_t rows = side == 0 ? h->m : h->n;
-    S_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, st));
-    if (timed) S_CUDA(h, cudaEventRecord(h->ev_half[side][0], st));
+    float *X = side == 0 ? h->d_U : h->d_V;
+    const size_t xbytes = sizeof(float) * (size_t)rows * h->f;
+    float *x_prev = nullptr, *x_cg = nullptr;
+    double *d_diff = nullptr;
+    int32_t *flags_save = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    auto cleanup = [&]() {
+        if (x_prev) cudaFree(x_prev);
+        if (x_cg) cudaFree(x_cg);
+        if (d_diff) cudaFree(d_diff);
+        if (flags_save) cudaFree(flags_save);
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    };
+    if (cudaMalloc(&x_prev, xbytes) != cudaSuccess || cudaMalloc(&x_cg, xbytes) != cudaSuccess ||
+        cudaMalloc(&d_diff, 2 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&flags_save, 4 * sizeof(int32_t)) != cudaSuccess) {
+        cleanup();
+        return fail(h, ALS_ERR_OUT_OF_MEMORY, "out of memory for the autotuner's factor copies");
+    }
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaError_t e = cudaSuccess;
+    bool timed_out = false;
+    for (size_t k = 0; k < h->plan[side].size() && e == cudaSuccess && !timed_out; ++k) {
+        SweepBucket &b = h->plan[side][k];
+        cudaMemcpyAsync(x_prev, X, xbytes, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(flags_save, h->d_flags, 4 * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+        cudaEventRecord(ev[0], st);
+        e = launch_bucket(h, side, b, ALS_SOLVE_CG_FP32, (int)k, launches);
+        cudaEventRecord(ev[1], st);
+        if (e != cudaSuccess) break;
+        cudaMemcpyAsync(x_cg, X, xbytes, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(X, x_prev, xbytes, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(h->d_flags, flags_save, 4 * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+        cudaEventRecord(ev[2], st);
+        e = launch_bucket(h, side, b, ALS_SOLVE_CHOLESKY, (int)k, launches);
+        cudaEventRecord(ev[3], st);
+        if (e != cudaSuccess) break;
+        e = launch_bucket_diff(h->d_order[side], b.lo, b.hi, X, x_cg, h->f, d_diff, st);
+        ++*launches;
+        double diff[2] = {0.0, 0.0};
+        int32_t fl[4] = {0, 0, 0, 0};
+        if (e == cudaSuccess) e = cudaMemcpyAsync(diff, d_diff, sizeof(diff), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) break;
+        if (fl[2]) {  // a bounded wait ran out: stop; check_sweep_flags reports the timeout
+            timed_out = true;
+            break;
+        }
+        cudaEventElapsedTime(&b.ms_cg, ev[0], ev[1]);
+        cudaEventElapsedTime(&b.ms_chol, ev[2], ev[3]);
+        b.rel = diff[1] > 0.0 ? (float)std::sqrt(diff[0] / diff[1]) : 0.f;
+        b.solver = (b.ms_cg < b.ms_chol && b.rel <= AUTO_TOL) ? ALS_SOLVE_CG_FP32
+                                                               : ALS_SOLVE_CHOLESKY;
+        h->cls_solver[side][b.cls] = b.solver;
+    }
+    cleanup();
+    if (e != cudaSuccess) return fail(h, ALS_ERR_CUDA, std::string("autotuner: ") + cudaGetErrorString(e));
+    if (!timed_out) h->tuned[side] = true;
+    return ALS_OK;
+}
+
+// Enqueue one half-sweep on the handle's stream, bracketed by the side's timing events: the BF16
+// table for the tensor-core path, then one launch per bucket of the side's plan.  No host
+// synchronisation (except the autotuner's one tuning sweep), so an epoch can be graph-captured.
+// The status words are zeroed by the caller once per call, so a timeout on either side survives
+// until check_sweep_flags reads them.
+als_status run_half_sweep(als_handle *h, int side) {
+    cudaStream_t st = h->stream;
+    if (h->plan[side].empty()) build_plan(h, side);
+    S_CUDA(h, record_event(h->ev_half[side][0], st));
     int launches = 0;
-    if (h->precision == ALS_PREC_FP32) {
-        SweepArgs a{};
-        a.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
-        a.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
-        a.val = side == 0 ? h->d_csr_val : h->d_csc_val;
-        a.Y = side == 0 ? h->d_V : h->d_U;
-        a.X = side == 0 ? h->d_U : h->d_V;
-        a.order = h->d_order[side];
-        a.row_begin = 0;
-        a.row_end = (int32_t)rows;
-        a.f = h->f;
-        a.lambda = h->cfg.lambda;
-        a.solve = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
-        a.cg_iters = h->cfg.cg_steps;
-        a.cg_tol = h->cfg.cg_tol;
-        a.flags = h->d_flags;
-        S_CUDA(h, launch_sweep_fp32(a, st, &launches));
-    } else {
+    if (h->precision != ALS_PREC_FP32) {
         std::string why;
-        als_status s = tc_half_sweep(h, side, &launches, &why);
+        als_status s = tc_quantise(h, side, &launches, &why);
         if (s != ALS_OK) return fail(h, s, why);
     }
-    if (timed) {
-        S_CUDA(h, cudaEventRecord(h->ev_half[side][1], st));
-        S_CUDA(h, cudaEventSynchronize(h->ev_half[side][1]));
-        float ms = 0.f;
-        S_CUDA(h, cudaEventElapsedTime(&ms, h->ev_half[side][0], h->ev_half[side][1]));
-        h->stage_ms[side] = ms;
+    const bool tuning = !h->tuned[side] && h->sweeps[side] >= 1;
+    ++h->sweeps[side];
+    if (tuning) {
+        als_status s = tune_side(h, side, &launches);
+        if (s != ALS_OK) return s;
+    } else {
+        for (size_t k = 0; k < h->plan[side].size(); ++k)
+            S_CUDA(h, launch_bucket(h, side, h->plan[side][k], h->plan[side][k].solver, (int)k,
+                                    &launches));
     }
+    S_CUDA(h, record_event(h->ev_half[side][1], st));
     h->counters[0] = launches;
+    return ALS_OK;
+}
+
+// After the stream has been synchronised: the side's last half-sweep time.
+als_status read_stage_ms(als_handle *h, int side) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev_half[side][0], h->ev_half[side][1]) == cudaSuccess) {
+        h->stage_ms[side] = ms;
+    } else {
+        h->stage_ms[side] = -1.0;  // not measurable: reported as negative, not as a failure
+        cudaGetLastError();
+    }
+    return ALS_OK;
+}
+
+// `iters` epochs.  Once the kernel plan is final (first epoch run; under ALS_SOLVE_AUTO the
+// tuning sweeps done) and use_graph is set, an epoch is captured into a CUDA graph once and
+// replayed: one launch call per epoch instead of one per kernel and memset.
+als_status run_epochs(als_handle *h, int32_t iters) {
+    cudaStream_t st = h->stream;
+    int epoch_launches = 0;
+    for (int32_t it = 0; it < iters; ++it) {
+        const bool graphable = h->cfg.use_graph && h->eager_epochs > 0 &&
+                               plan_final(h);
+        if (graphable && !h->graph_exec) {
+            S_CUDA(h, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            als_status s = run_half_sweep(h, 0);
+            epoch_launches = (int)h->counters[0];
+            if (s == ALS_OK) s = run_half_sweep(h, 1);
+            epoch_launches += (int)h->counters[0];
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (s != ALS_OK) {
+                if (g) cudaGraphDestroy(g);
+                return s;
+            }
+            S_CUDA(h, e);
+            h->graph = g;
+            S_CUDA(h, cudaGraphInstantiate(&h->graph_exec, g, 0));
+            h->counters[0] = epoch_launches;
+        }
+        if (graphable) {
+            S_CUDA(h, cudaGraphLaunch(h->graph_exec, st));
+        } else {
+            als_status s = run_half_sweep(h, 0);
+            if (s != ALS_OK) return s;
+            int launches = (int)h->counters[0];
+            s = run_half_sweep(h, 1);
+            if (s != ALS_OK) return s;
+            h->counters[0] += launches;
+            ++h->eager_epochs;
+        }
+    }
     return ALS_OK;
 }
 
@@ -123,17 +337,38 @@ extern "C" als_status als_get_plan(const als_handle *h, int32_t side, int32_t *l
                                    int32_t *solver, int32_t *nb) {
     if (!h || !nb || (side != 0 && side != 1))
         return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
-    if (h->precision == ALS_PREC_FP32) {
+    const int32_t fkind = h->precision == ALS_PREC_FP32 ? 0 : h->precision == ALS_PREC_FP8 ? 2 : 1;
+    const std::vector<SweepBucket> &plan = h->plan[side];
+    if (plan.empty()) {  // no sweep yet: the plan the next sweep starts from
         if (*nb >= 1) {
             if (lo) lo[0] = 0;
-            if (kind) kind[0] = 0;
-            if (solver) solver[0] = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY
-                                                                        : h->cfg.solve_type;
+            if (kind) kind[0] = fkind;
+            if (solver) solver[0] = autotuned(h) ? ALS_SOLVE_CHOLESKY : h->cfg.solve_type;
         }
         *nb = 1;
         return ALS_OK;
     }
-    return tc_get_plan(h, side, lo, kind, solver, nb);
+    for (int32_t k = 0; k < (int32_t)plan.size() && k < *nb; ++k) {
+        if (lo) lo[k] = plan[k].lo;
+        if (kind) kind[k] = fkind;
+        if (solver) solver[k] = plan[k].solver;
+    }
+    *nb = (int32_t)plan.size();
+    return ALS_OK;
+}
+
+extern "C" als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg,
+                                     float *ms_chol, float *rel, int32_t *nb) {
+    if (!h || !nb || (side != 0 && side != 1))
+        return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
+    const std::vector<SweepBucket> &plan = h->plan[side];
+    for (int32_t k = 0; k < (int32_t)plan.size() && k < *nb; ++k) {
+        if (ms_cg) ms_cg[k] = plan[k].ms_cg;
+        if (ms_chol) ms_chol[k] = plan[k].ms_chol;
+        if (rel) rel[k] = plan[k].rel;
+    }
+    *nb = (int32_t)plan.size();
+    return ALS_OK;
 }
 
 extern "C" als_status als_user_halfsweep_adjoint(als_handle *h, const als_coo_view *heldout,

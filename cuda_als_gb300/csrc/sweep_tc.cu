@@ -34,7 +34,9 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cmath>
 #include <string>
+#include <vector>
 
 #include "handle.h"
 #include "internal.h"
@@ -58,7 +60,6 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
 }  // namespace tcg
 }  // namespace als
 
-
 // ------------------------------------------------------------------------------------- host side
 
 using namespace als;
@@ -71,12 +72,10 @@ static int tcg_solver(int solve_type) {
     default: return tcg::SOLVER_CHOL;
     }
 }
-
 struct TcState {
-    tcg::Geometry geo{};
-    int solver = 1;
+    tcg::Geometry geo[3];  // per solver (CG, Cholesky, LU)
     __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
-    int32_t *d_work = nullptr;
+    int32_t *d_work = nullptr;                     // one row counter per bucket
     int num_sms = 0;
     cudaEvent_t ev_q[2] = {nullptr, nullptr};
 };
@@ -100,29 +99,34 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     }
     TcState *t = new TcState();
     h->tc = t;
-    t->solver = tcg_solver(h->cfg.solve_type);
-    t->geo = tcg::geometry(h->f, t->solver);
+    size_t smem_max = 0;
+    for (int sv = 0; sv < 3; ++sv) {
+        t->geo[sv] = tcg::geometry(h->f, sv);
+        smem_max = std::max(smem_max, t->geo[sv].smem);
+    }
     t->num_sms = sms;
     const int64_t opp[2] = {h->n, h->m};  // side 0 gathers V rows, side 1 gathers U rows
     for (int s = 0; s < 2; ++s) {
-        const size_t bytes = sizeof(__nv_bfloat16) * (size_t)(opp[s] + 1) * t->geo.fst;
+        const size_t bytes = sizeof(__nv_bfloat16) * (size_t)(opp[s] + 1) * t->geo[0].fst;
         if (cudaMalloc(&t->d_bf[s], bytes) != cudaSuccess ||
             cudaMemset(t->d_bf[s], 0, bytes) != cudaSuccess) {
             *why = "out of memory for the BF16 factor tables";
             return ALS_ERR_OUT_OF_MEMORY;
         }
     }
-    if (cudaMalloc(&t->d_work, sizeof(int32_t) * 4) != cudaSuccess) {
+    if (cudaMalloc(&t->d_work, sizeof(int32_t) * 8) != cudaSuccess) {
         *why = "out of memory";
         return ALS_ERR_OUT_OF_MEMORY;
     }
-    for (int k = 0; k < 2; ++k) cudaEventCreate(&t->ev_q[k]);
+    for (auto &e : t->ev_q) cudaEventCreate(&e);
+    // sets every solver variant's shared-memory limit, which also loads them now, so no launch
+    // inside a timed region (the autotuner's) loads a module
     cudaError_t e;
-    switch (t->geo.fp) {
-    case 32: e = tcg::configure_32(t->geo.smem); break;
-    case 64: e = tcg::configure_64(t->geo.smem); break;
-    case 112: e = tcg::configure_112(t->geo.smem); break;
-    default: e = tcg::configure_128(t->geo.smem); break;
+    switch (t->geo[0].fp) {
+    case 32: e = tcg::configure_32(smem_max); break;
+    case 64: e = tcg::configure_64(smem_max); break;
+    case 112: e = tcg::configure_112(smem_max); break;
+    default: e = tcg::configure_128(smem_max); break;
     }
     if (e != cudaSuccess) {
         *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
@@ -147,70 +151,71 @@ void tc_invalidate_graphs(als_handle *) {}
 
 als_status tc_values_changed(als_handle *) { return ALS_OK; }
 
-als_status tc_half_sweep(als_handle *h, int side, int *launches, std::string *why) {
+// The BF16 copy of the table a side gathers (features f..fst-1 zero, plus an all-zero last row
+// that pads ragged stages).
+als_status tc_quantise(als_handle *h, int side, int *launches, std::string *why) {
     TcState *t = h->tc;
-    cudaStream_t st = h->stream;
-    const int64_t rows = side == 0 ? h->m : h->n;
     const int64_t opp = side == 0 ? h->n : h->m;
     const float *Y = side == 0 ? h->d_V : h->d_U;
-    cudaEventRecord(t->ev_q[0], st);
-    {
-        const int64_t total = opp * t->geo.fst;
-        int grid = (int)std::min<int64_t>((total + 255) / 256, (int64_t)t->num_sms * 8);
-        tcg::quantise_bf16_kernel<<<grid, 256, 0, st>>>(Y, opp, h->f, t->geo.fst, t->d_bf[side]);
-        ++*launches;
-    }
-    cudaEventRecord(t->ev_q[1], st);
-    cudaMemsetAsync(t->d_work, 0, sizeof(int32_t), st);
-    tcg::Params p{};
-    p.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
-    p.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
-    p.val = side == 0 ? h->d_csr_val : h->d_csc_val;
-    p.order = h->d_order[side];
-    p.Ybf = t->d_bf[side];
-    p.X = side == 0 ? h->d_U : h->d_V;
-    p.work = t->d_work;
-    p.flags = h->d_flags;
-    p.nrows = (int32_t)rows;
-    p.zero_row = (int32_t)opp;
-    p.f = h->f;
-    p.fst = t->geo.fst;
-    p.ng = t->geo.ng;
-    p.acc_stride = t->geo.acc_stride;
-    p.tmem_cols = t->geo.tmem_cols;
-    p.nbuf = t->geo.nbuf;
-    p.nepi = t->geo.nepi;
-    p.solve = t->solver;
-    p.cg_iters = h->cfg.cg_steps;
-    p.refine_steps = h->cfg.refine_steps;
-    p.lambda = h->cfg.lambda;
-    p.cg_tol = h->cfg.cg_tol;
-    p.cond_threshold = h->cfg.cond_threshold;
-    const int grid = (int)std::min<int64_t>(rows, t->num_sms);
-    switch (t->geo.fp) {
-    case 32: tcg::launch_32(p, t->geo, grid, st); break;
-    case 64: tcg::launch_64(p, t->geo, grid, st); break;
-    case 112: tcg::launch_112(p, t->geo, grid, st); break;
-    default: tcg::launch_128(p, t->geo, grid, st); break;
-    }
+    record_event(t->ev_q[0], h->stream);
+    const int64_t total = opp * t->geo[0].fst;
+    const int grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>((total + 255) / 256, (int64_t)t->num_sms * 8));
+    tcg::quantise_bf16_kernel<<<grid, 256, 0, h->stream>>>(Y, opp, h->f, t->geo[0].fst,
+                                                           t->d_bf[side]);
     ++*launches;
-    cudaError_t e = cudaGetLastError();
+    record_event(t->ev_q[1], h->stream);
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
-        *why = std::string("sweep_tc_kernel launch: ") + cudaGetErrorString(e);
+        *why = std::string("quantise_bf16_kernel: ") + cudaGetErrorString(e);
         return ALS_ERR_CUDA;
     }
     return ALS_OK;
 }
 
-als_status tc_get_plan(const als_handle *h, int side, int32_t *lo, int32_t *kind,
-                       int32_t *solver, int32_t *nb) {
-    (void)side;
-    if (*nb >= 1) {
-        if (lo) lo[0] = 0;
-        if (kind) kind[0] = h->precision == ALS_PREC_FP8 ? 2 : 1;
-        if (solver) solver[0] = h->cfg.solve_type == ALS_SOLVE_AUTO ? ALS_SOLVE_CHOLESKY
-                                                                    : h->cfg.solve_type;
+// One persistent launch over the rows order[lo..hi) of the side with the given ALS_SOLVE_*
+// solver; `slot` picks the bucket's row counter.
+cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t hi, int solve,
+                             int slot, int *launches) {
+    const TcState *t = h->tc;
+    cudaStream_t st = h->stream;
+    const int solver = tcg_solver(solve);
+    const tcg::Geometry &g = t->geo[solver];
+    const int64_t opp = side == 0 ? h->n : h->m;
+    cudaError_t e = cudaMemsetAsync(t->d_work + slot, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess) return e;
+    tcg::Params p{};
+    p.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
+    p.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
+    p.val = side == 0 ? h->d_csr_val : h->d_csc_val;
+    p.order = h->d_order[side] + lo;
+    p.Ybf = t->d_bf[side];
+    p.X = side == 0 ? h->d_U : h->d_V;
+    p.work = t->d_work + slot;
+    p.flags = h->d_flags;
+    p.nrows = hi - lo;
+    p.zero_row = (int32_t)opp;
+    p.f = h->f;
+    p.fst = g.fst;
+    p.ng = g.ng;
+    p.acc_stride = g.acc_stride;
+    p.tmem_cols = g.tmem_cols;
+    p.nbuf = g.nbuf;
+    p.nepi = g.nepi;
+    p.solve = solver;
+    p.cg_iters = h->cfg.cg_steps;
+    p.refine_steps = h->cfg.refine_steps;
+    p.lambda = h->cfg.lambda;
+    p.cg_tol = h->cfg.cg_tol;
+    p.cond_threshold = h->cfg.cond_threshold;
+    const int grid = (int)std::min<int64_t>(p.nrows, t->num_sms);
+    if (grid <= 0) return cudaSuccess;
+    switch (g.fp) {
+    case 32: tcg::launch_32(p, g, grid, st); break;
+    case 64: tcg::launch_64(p, g, grid, st); break;
+    case 112: tcg::launch_112(p, g, grid, st); break;
+    default: tcg::launch_128(p, g, grid, st); break;
     }
-    *nb = 1;
-    return ALS_OK;
+    ++*launches;
+    return cudaGetLastError();
 }

@@ -90,8 +90,8 @@ typedef struct als_config {
     float cond_threshold;         /* diag-ratio estimate above which the residual is FP64       */
     int32_t cg_steps;             /* CG iterations (reference CG_ITER = 6, als_model.cu:16)     */
     float cg_tol;                 /* CG exit when r'r < cg_tol (reference CG_ERROR, cg.cu:32)   */
-    int32_t use_graph;            /* capture each half-sweep in a CUDA graph                    */
-    int32_t autotune;             /* time candidate kernels per nnz bucket on the first sweep   */
+    int32_t use_graph;            /* replay each epoch from a CUDA graph once the plan is final */
+    int32_t autotune;             /* ALS_SOLVE_AUTO: 0 tune once per handle, 1 at every init    */
     int32_t device;               /* CUDA device ordinal                                        */
 } als_config;
 
@@ -239,6 +239,14 @@ als_status als_get_counters(const als_handle *h, int64_t out[3]);
  * 1 = BF16 tcgen05, 2 = FP8 tcgen05) and solver[b] (ALS_SOLVE_*).  nb in: capacity, out: count. */
 als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t *kind,
                         int32_t *solver, int32_t *nb);
+
+/* The autotuner's measurements per bucket of the plan (ALS_SOLVE_AUTO, tensor-core precisions):
+ * ms_cg[b] / ms_chol[b] = CUDA-event time of the bucket's launch with each solver on the tuning
+ * sweep (the side's second half-sweep, both from the same warm start), rel[b] = ||x_cg - x_chol||
+ * / ||x_chol|| over the bucket's rows.  Negative entries: not tuned.  nb in: capacity, out: count.
+ * Buckets are the rows of degree >= 8f, f <= degree < 8f and degree < f, in that order. */
+als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg, float *ms_chol,
+                          float *rel, int32_t *nb);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Adjoint of the user half-sweep (no reference counterpart; required by the build's spec)     */

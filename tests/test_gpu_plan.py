@@ -1,0 +1,128 @@
+"""nnz buckets, the Cholesky/CG autotuner (ALS_SOLVE_AUTO) and CUDA-graph epochs, through the C ABI.
+
+Workload 2's shape (lognormal row degrees, Zipf columns, f = 64): the buckets must
+equal the host's degree counts exactly, the tuner's choice must follow its rule from its own
+measurements, training under AUTO must reach the plain-FP32 Cholesky test RMSE, and an epoch
+replayed from the captured graph must give the same bits as the same epoch launched eagerly.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cuda_als_gb300 as ca
+
+pytestmark = pytest.mark.gpu
+
+AUTO_TOL = 2e-2          # the tuner's CG-vs-Cholesky agreement bound (sweep.cpp)
+TOL_RMSE = 2e-3          # test RMSE after training vs plain FP32 Cholesky
+
+
+def workload2(scale=0.1):
+    tr, te, info = ca.synth_generate(2, scale=scale)
+    return tr, te, info
+
+
+def model(tr, te, info, solve, precision, iters=10, **opt):
+    return ca.als_model(tr, te, info["f"], info["lambda"], iters,
+                        ca.CALCULATE_VTVS_TYPE.SMEM_ROW_MAJOR, solve, precision=int(precision),
+                        **opt)
+
+
+def expected_cuts(ptr, f):
+    deg = np.diff(np.asarray(ptr, np.int64))
+    heavy = int((deg >= 8 * f).sum())
+    mid = int(((deg >= f) & (deg < 8 * f)).sum())
+    cuts = [0, heavy, heavy + mid]
+    los = [c for k, c in enumerate(cuts) if (cuts + [len(deg)])[k + 1] > c]
+    return los
+
+
+@pytest.mark.parametrize("precision", [ca.PRECISION.BF16, ca.PRECISION.FP32])
+def test_auto_buckets_follow_degrees_and_tuner_rule(precision):
+    tr, te, info = workload2()
+    f = info["f"]
+    ptr_u = tr.h_csr_row_ptrs
+    cptr = np.zeros(info["n"] + 1, np.int64)
+    np.add.at(cptr, tr.h_csr_coo_col_idxs.astype(np.int64) + 1, 1)
+    ptr_v = np.cumsum(cptr)
+    with model(tr, te, info, ca.SOLVE_TYPE.AUTO, precision, iters=3) as mdl:
+        mdl.init_factors()
+        mdl.iterate(3)
+        for side, ptr in ((0, ptr_u), (1, ptr_v)):
+            plan = mdl.plan(side)
+            assert [b["lo"] for b in plan] == expected_cuts(ptr, f)
+            tuning = mdl.tuning(side)
+            assert len(tuning) == len(plan)
+            for b, t in zip(plan, tuning):
+                assert t["ms_cg"] > 0 and t["ms_cholesky"] > 0 and t["rel_diff"] >= 0
+                want_cg = t["ms_cg"] < t["ms_cholesky"] and t["rel_diff"] <= AUTO_TOL
+                assert b["solver"] == (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32 if want_cg
+                                       else ca.SOLVE_TYPE.CHOLESKY)
+                assert b["kind"] == (0 if precision == ca.PRECISION.FP32 else 1)
+        assert mdl.counters()["flagged_rows"] == 0
+
+
+def test_fixed_solver_is_one_bucket():
+    tr, te, info = workload2()
+    with model(tr, te, info, ca.SOLVE_TYPE.CHOLESKY, ca.PRECISION.BF16, iters=1) as mdl:
+        mdl.init_factors()
+        mdl.iterate(2)
+        for side in (0, 1):
+            assert mdl.plan(side) == [{"lo": 0, "kind": 1, "solver": int(ca.SOLVE_TYPE.CHOLESKY)}]
+            assert all(t["ms_cg"] < 0 for t in mdl.tuning(side))
+
+
+@pytest.mark.parametrize("precision", [ca.PRECISION.BF16, ca.PRECISION.FP32])
+def test_auto_training_reaches_fp32_cholesky_rmse(precision):
+    """Full-size workload 2 (69,878 x 10,677, 10M ratings, f = 64), 10 iterations.  (Scaled-down
+    copies of it over-fit, test RMSE ~1.34, where 6-step CG itself lands 2e-3 from Cholesky.)"""
+    tr, te, info = workload2(scale=1.0)
+    with model(tr, te, info, ca.SOLVE_TYPE.CHOLESKY, ca.PRECISION.FP32) as ref:
+        ref.train()
+        r_ref = ref.rsme_test()
+    with model(tr, te, info, ca.SOLVE_TYPE.AUTO, precision) as mdl:
+        mdl.train()
+        r = mdl.rsme_test()
+    assert abs(r - r_ref) < TOL_RMSE
+
+
+@pytest.mark.parametrize("precision,solve", [
+    (ca.PRECISION.BF16, ca.SOLVE_TYPE.CHOLESKY),
+    (ca.PRECISION.BF16, ca.SOLVE_TYPE.AUTO),
+    (ca.PRECISION.FP32, ca.SOLVE_TYPE.CUMF_ALS_CG_FP32),
+])
+def test_graph_epochs_match_eager_bits(precision, solve):
+    """Rows are independent and each row's arithmetic has a fixed order, so a replayed epoch must
+    reproduce the eager epoch bit for bit (whichever SM takes which row)."""
+    tr, te, info = workload2()
+    out = []
+    for use_graph in (0, 1):
+        with model(tr, te, info, solve, precision, use_graph=use_graph) as mdl:
+            mdl.init_factors()
+            for _ in range(5):
+                mdl.iterate(1)
+            out.append(mdl.get_factors())
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_graph_survives_value_update_and_reload():
+    """update_values keeps the captured epoch (same buffers); reload drops it and rebuilds the
+    buckets; both must match a fresh model on the new data."""
+    tr, te, info = workload2()
+    vals2 = (tr.h_csr_coo_vals[::-1]).copy()
+    with model(tr, te, info, ca.SOLVE_TYPE.CHOLESKY, ca.PRECISION.BF16) as mdl:
+        mdl.init_factors()
+        mdl.iterate(3)
+        mdl.update_values(vals2)
+        mdl.init_factors()
+        mdl.iterate(3)
+        got = mdl.get_factors()
+    tr2 = ca.host_sparse_matrix(info["m"], info["n"], len(vals2)).set_csr(
+        tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, vals2)
+    with model(tr2, te, info, ca.SOLVE_TYPE.CHOLESKY, ca.PRECISION.BF16) as mdl:
+        mdl.init_factors()
+        mdl.iterate(3)
+        want = mdl.get_factors()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
