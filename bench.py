@@ -2,14 +2,15 @@
 """ALS epoch benchmark on the 480,189 x 17,770, 100M-rating workload (f = 100, lambda = 0.048).
 
 One step = one ALS epoch (U half-sweep over the CSR, then V half-sweep over the CSC) of the
-library's sweep, inputs resident in HBM.  The timed region is K steps bracketed by a barrier and
-a device synchronize, timed with CUDA events on the stream the library launches on.  The inputs
-(an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors) are far larger than the 129 MB L2, so no
-flush is needed between steps.
+library's sweep, inputs resident in HBM; by default the BF16 tensor-core sweep with the per-bucket
+Cholesky/CG autotuner (ALS_SOLVE_AUTO), epochs replayed from the captured CUDA graph.  The timed
+region is K steps bracketed by a barrier and a device synchronize, timed with CUDA events on the
+stream the library launches on.  The inputs (an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors)
+are far larger than the 129 MB L2, so no flush is needed between steps.
 
 The same run also measures, on the same data:
-  * the plain-FP32 sweep (the comparison of the metric), epoch ms and test RMSE after the
-    configured 10 iterations for both precisions;
+  * the plain-FP32 Cholesky sweep (the comparison of the metric) and the BF16 Cholesky sweep with
+    one refinement step, epoch ms and test RMSE after the configured 10 iterations;
   * e2e: the same epoch through the C ABI with HOST buffers: each step re-uploads the ratings
     from pinned memory (als_reload: H2D, validation, GPU transpose, degree orders), runs the
     epoch and reads back both factor tables and the test RMSE;
@@ -52,13 +53,16 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
     p.add_argument("--scale", type=float, default=1.0)
-    p.add_argument("--precision", choices=["bf16", "fp32", "fp8"], default=None)
-    p.add_argument("--solve", choices=["lu", "cg", "cholesky", "auto"], default="cholesky")
+    p.add_argument("--precision", choices=["bf16", "fp32"], default=None)
+    p.add_argument("--solve", choices=["lu", "cg", "cholesky", "auto"], default="auto",
+                   help="solver of the measured sweep (default: per-bucket autotuned)")
     p.add_argument("--iters", type=int, default=None, help="iterations for the RMSE comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--no-compare", action="store_true", help="skip the plain-FP32 comparison")
-    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip the plain-FP32 Cholesky and BF16 Cholesky+refinement comparisons")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="host time of the CPU-baseline sample (lands between 0.6x and ~1.5x)")
     return p.parse_args()
 
 
@@ -128,6 +132,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def load_traffic(args, side, prec_name):
+    """DRAM bytes (read + write) of one half-sweep of this workload, from the committed ncu
+    summary (profiles/dram_traffic.txt: `config scale precision solve side bytes` lines), or
+    None when no capture covers it."""
+    f = ROOT / "profiles" / "dram_traffic.txt"
+    if not f.exists():
+        return None
+    for ln in f.read_text().splitlines():
+        parts = ln.split()
+        if len(parts) == 6 and not ln.startswith("#"):
+            c, sc, pr, sv, sd, b = parts
+            if (int(c) == args.config and float(sc) == args.scale and pr == prec_name
+                    and sv == args.solve and sd == side):
+                return float(b)
+    return None
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -174,9 +195,13 @@ def cpu_epoch_estimate(tr, info, seconds, seed=0):
         t2 = time.perf_counter()
         return (t1 - t0) * m / len(su) + (t2 - t1) * n / len(sv), t2 - t0, len(su), len(sv)
 
-    est, spent, _, _ = timed(0.002)
-    frac = min(1.0, 0.002 * max(1.0, seconds / max(spent, 1e-3)))
+    frac = 0.002
     est, spent, nu, nv = timed(frac)
+    # grow the sample until it takes at least 60% of the target (per-call overheads make the
+    # first scaling land short)
+    while spent < 0.6 * seconds and frac < 1.0:
+        frac = min(1.0, frac * min(8.0, 1.2 * seconds / max(spent, 1e-3)))
+        est, spent, nu, nv = timed(frac)
     return {"value": est * 1e3, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"random {nu} of {m} rows (U side) and {nv} of {n} rows (V side), "
                       f"{spent:.1f} s of host time, scaled by rows to one epoch"}
@@ -223,7 +248,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, config 3 shapes)",
+        "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded, workload {args.config} shapes)",
         "config": config_dict(args, info, "fp32-host"),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores,
                          "kind": "port", "sample": sample},
@@ -266,15 +291,14 @@ def run_ours(args):
     iters = args.iters if args.iters is not None else 10
     solve = {"lu": ca.SOLVE_TYPE.LU, "cg": ca.SOLVE_TYPE.CUMF_ALS_CG_FP32,
              "cholesky": ca.SOLVE_TYPE.CHOLESKY, "auto": ca.SOLVE_TYPE.AUTO}[args.solve]
-    prec_name = args.precision
-    if prec_name is None:
-        prec_name = "bf16" if f <= 128 and _tc_available(ca) else "fp32"
-    prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16, "fp8": ca.PRECISION.FP8}[prec_name]
+    prec_name = args.precision or ("bf16" if f <= 128 else "fp32")
+    prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16}[prec_name]
     stream = torch.cuda.Stream()
 
-    def make(precision):
-        mdl = ca.als_model(tr, te, f, lam, iters, ca.CALCULATE_VTVS_TYPE.SMEM_ROW_MAJOR, solve,
-                           32, 1, 1, precision=int(precision), device=local)
+    def make(precision, how=None):
+        mdl = ca.als_model(tr, te, f, lam, iters, ca.CALCULATE_VTVS_TYPE.SMEM_ROW_MAJOR,
+                           solve if how is None else how, 32, 1, 1, precision=int(precision),
+                           device=local)
         mdl.set_stream(stream.cuda_stream)
         return mdl
 
@@ -312,26 +336,39 @@ def run_ours(args):
     clocks = clk.summary()
     stage = model.stage_ms()
     counters = model.counters()
-    plan = model.plan(0) if prec != ca.PRECISION.FP32 else None
+    plan = {side: [dict(b, **t) for b, t in zip(model.plan(k), model.tuning(k) or
+                                                [{}] * len(model.plan(k)))]
+            for k, side in ((0, "U"), (1, "V"))}
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     rmse = rmse_after(model, iters)
 
-    # ---- plain FP32 on the same data (the metric's comparison)
-    fp32 = None
-    if not args.no_compare and prec != ca.PRECISION.FP32:
-        ref = make(ca.PRECISION.FP32)
+    # ---- the metric's comparison: plain FP32 Cholesky on the same data; and the BF16 Cholesky
+    # sweep with one refinement step (FP64 residual on ill-conditioned rows), the configuration
+    # the >= 3x target names, when the measured sweep is not already that
+    def compare(precision, how):
+        ref = make(precision, how)
         ref.init_factors()
-        ref.iterate(2)
-        fms = time_epochs(ref, max(2, min(args.steps, 3)))
-        fstage = ref.stage_ms()
-        frmse = rmse_after(ref, iters)
-        fp32 = {"ms_per_epoch": round(fms, 3), "U_ms": round(fstage["U"], 3),
-                "V_ms": round(fstage["V"], 3), "test_rmse_after_iters": frmse,
-                "speedup": round(fms / ms, 3), "rmse_delta": abs(rmse - frmse)}
+        ref.iterate(3)
+        cms = time_epochs(ref, max(2, min(args.steps, 3)))
+        cst = ref.stage_ms()
+        crmse = rmse_after(ref, iters)
         ref.close()
+        return cms, {"ms_per_epoch": round(cms, 3), "U_ms": round(cst["U"], 3),
+                     "V_ms": round(cst["V"], 3), "test_rmse_after_iters": crmse}
+
+    fp32 = chol = None
+    if not args.no_compare and prec != ca.PRECISION.FP32:
+        fms, fp32 = compare(ca.PRECISION.FP32, ca.SOLVE_TYPE.CHOLESKY)
+        fp32.update(solve="cholesky", speedup=round(fms / ms, 3),
+                    rmse_delta=abs(rmse - fp32["test_rmse_after_iters"]))
+        if solve != ca.SOLVE_TYPE.CHOLESKY:
+            cms, chol = compare(prec, ca.SOLVE_TYPE.CHOLESKY)
+            chol.update(refine_steps=1, speedup_vs_fp32=round(fms / cms, 3),
+                        rmse_delta_vs_fp32=abs(chol["test_rmse_after_iters"] -
+                                               fp32["test_rmse_after_iters"]))
 
     # ---- e2e through the C ABI with host buffers
     e2e = None
@@ -368,10 +405,13 @@ def run_ours(args):
     dom_flops = gram_u + rhs_u
     achieved = dom_flops / (dom_ms * 1e-3) / 1e12
     gram_tflops = (gram_u + gram_v) / (ms * 1e-3) / 1e12
+    traffic = load_traffic(args, dom_side, prec_name)
     roofline = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak_bf16,
-                "unit": "TFLOP/s", "frac": round(achieved / peak_bf16, 4), "traffic": None,
-                "kernel": f"fused half-sweep ({dom_side} side), Gram+RHS flops "
-                          f"nnz*f*(f+1)+2*nnz*f per launch over its CUDA-event time",
+                "unit": "TFLOP/s", "frac": round(achieved / peak_bf16, 4),
+                "traffic": traffic,
+                "kernel": f"fused half-sweep ({dom_side} side: BF16 quantise + one sweep_tc_kernel "
+                          f"launch per nnz bucket), Gram+RHS flops nnz*f*(f+1)+2*nnz*f over its "
+                          f"CUDA-event time",
                 "peak_source": f"bf16 dense, {peak_src}"}
     if prec == ca.PRECISION.FP32:
         roofline["note"] = "FP32 path runs on CUDA cores: the fraction is of the bf16 tensor peak"
@@ -380,35 +420,27 @@ def run_ours(args):
     if not args.no_cpu and rank == 0:
         cpu = cpu_epoch_estimate(tr, info, args.cpu_seconds)
 
-    launches = int(counters["launches"]) * 2 * args.steps
+    launches = int(counters["launches"]) * args.steps  # kernels per epoch (both halves) x steps
     line = {
         "metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": prec_name, "data": "synthetic (seeded, config 3 shapes; Netflix stand-in)",
+        "dtype": prec_name, "data": f"synthetic (seeded, workload {args.config} shapes"
+                                         + ("; Netflix stand-in)" if args.config == 3 else ")"),
         "config": config_dict(args, info, prec_name),
         "gram_tflops": round(gram_tflops, 3),
         "stage_ms": {k: round(v, 3) for k, v in stage.items()},
         "test_rmse_after_iters": rmse, "iters": iters,
-        "fp32_plain": fp32, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "fp32_plain": fp32, "bf16_cholesky_refined": chol, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks, "gpu_launches": launches,
         "flagged_rows": counters["flagged_rows"],
     }
-    if plan:
-        line["plan_U"] = plan
+    line["plan"] = plan
     model.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def _tc_available(ca) -> bool:
-    try:
-        cfg = ca.default_config()
-        return True if cfg is not None and os.environ.get("ALS_BENCH_FP32_ONLY") is None else False
-    except Exception:
-        return False
 
 
 def main():

@@ -294,6 +294,14 @@ static als_status validate_config(const als_config &c, std::string *why) {
         *why = "precision must be fp32, bf16 or fp8";
         return ALS_ERR_INVALID_ARG;
     }
+    if (p == ALS_PREC_FP8) {
+        // A per-row e4m3 scale of the gathered factors varies along the contraction (ratings), so
+        // it cannot be taken out of Y_u^T Y_u, and 8-bit tcgen05 operands want the K-major
+        // (ratings-contiguous) panel the gather does not produce; the BF16 path is the
+        // reduced-precision sweep of this library.
+        *why = "precision fp8 (e4m3 Gram) is not built; use bf16";
+        return ALS_ERR_UNSUPPORTED;
+    }
     if (p == ALS_PREC_FP32 && !fp32_supported(c.f)) {
         *why = "f too large for the FP32 path (max 231)";
         return ALS_ERR_UNSUPPORTED;

@@ -69,7 +69,7 @@ enum {
     ALS_PREC_FROM_VTVS = -1,   /* derive from calculate_vtvs_type (0-4 -> FP32, 5-7 -> BF16)       */
     ALS_PREC_FP32 = 0,
     ALS_PREC_BF16 = 1,
-    ALS_PREC_FP8 = 2           /* e4m3 with a per-row scale                                        */
+    ALS_PREC_FP8 = 2           /* e4m3 with a per-row scale: reserved, rejected with UNSUPPORTED   */
 };
 
 /* Model configuration.  The first block holds the reference's INI keys and als_model ctor

@@ -145,6 +145,17 @@ def test_no_device_fails_loudly():
                       t["R_train_csr_data"])
 
 
+def test_fp8_precision_is_refused_before_any_device_work(toy):
+    """FP8 (e4m3) is reserved in the ABI but not built: the configuration is rejected as
+    UNSUPPORTED, never silently run at another precision."""
+    tr = ca.host_sparse_matrix(toy["m"], toy["n"], len(toy["R_train_csr_data"])).set_csr(
+        toy["R_train_csr_indptr"], toy["R_train_csr_indices"], toy["R_train_csr_data"])
+    with pytest.raises(ca.ALSError) as e:
+        ca.als_model(tr, None, 8, 0.05, 1, precision=int(ca.PRECISION.FP8))
+    assert e.value.status == ca.Status.UNSUPPORTED
+    assert "fp8" in str(e.value)
+
+
 @pytest.mark.parametrize("config,scale", [(1, 1.0), (2, 0.05), (3, 0.03), (4, 0.03), (5, 0.03)])
 def test_synthetic_workload_invariants(config, scale):
     tr, te, info = ca.synth_generate(config, scale=scale)
