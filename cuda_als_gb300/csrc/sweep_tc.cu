@@ -29,6 +29,7 @@
 //
 // Every wait is bounded by %globaltimer: a wait that runs out sets the status word, the kernel
 // drains its own MMAs and copies, frees TMEM and returns; the host reports ALS_ERR_TIMEOUT.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -73,6 +74,7 @@ static int tcg_solver(int solve_type) {
     }
 }
 struct TcState {
+    CUtensorMap tmap[2];   // [side]: TMA map of d_bf[side] (64-byte aligned member first)
     tcg::Geometry geo[3];  // per solver (CG, Cholesky, LU)
     __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
     int32_t *d_work = nullptr;                     // one row counter per bucket
@@ -81,6 +83,38 @@ struct TcState {
 };
 
 bool tc_path_supported(int f) { return f >= 1 && f <= tcg::MAXF; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// The gather map of a BF16 table of `rows` x fst: box = 64 features (128 bytes, the swizzle
+// span) x 1 row, as tile::gather4 requires; features past fst read as zero.
+static bool encode_table_map(CUtensorMap *map, void *table, int64_t rows, int fst) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)fst, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)fst * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[2] = {64, 1};
+    const cuuint32_t estride[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, table, dims, strides, box, estride,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 als_status tc_prepare(als_handle *h, std::string *why) {
     if (!tc_path_supported(h->f)) {
@@ -112,6 +146,10 @@ als_status tc_prepare(als_handle *h, std::string *why) {
             cudaMemset(t->d_bf[s], 0, bytes) != cudaSuccess) {
             *why = "out of memory for the BF16 factor tables";
             return ALS_ERR_OUT_OF_MEMORY;
+        }
+        if (!encode_table_map(&t->tmap[s], t->d_bf[s], opp[s] + 1, t->geo[0].fst)) {
+            *why = "cuTensorMapEncodeTiled failed for the BF16 table";
+            return ALS_ERR_CUDA;
         }
     }
     if (cudaMalloc(&t->d_work, sizeof(int32_t) * 8) != cudaSuccess) {
@@ -185,6 +223,7 @@ cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t 
     cudaError_t e = cudaMemsetAsync(t->d_work + slot, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     tcg::Params p{};
+    p.tmap = t->tmap[side];
     p.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
     p.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
     p.val = side == 0 ? h->d_csr_val : h->d_csc_val;

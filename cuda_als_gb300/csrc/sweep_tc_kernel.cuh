@@ -2,6 +2,7 @@
 // design); instantiated per padded size by sweep_tc_fp*.cu.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,6 +29,11 @@ constexpr int R_BYTES = 2 * ATOM_BYTES;      // K-major rating tile, N = 16 rows
 constexpr int STAGE_BYTES = TILE_BYTES + R_BYTES;
 constexpr int MAXF = 128;
 constexpr int MAX_NBUF = 4;
+// Producer metadata ring: each stage's column ids and ratings are copied into shared memory MD
+// stages ahead of its gathers (MR slots, MR > MD), so their HBM latency never stalls the gathers.
+constexpr int MD = 12;
+constexpr int MR = 16;
+constexpr int MRING_BYTES = MR * KC * 8 + MR * 16;   // column ids, ratings, Meta per slot
 enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2 };
 constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
 
@@ -39,6 +45,9 @@ struct Meta {  // per stage / per accumulator
 };
 
 struct Params {
+    // 2-D map of the BF16 table (fst features x n_opp + 1 rows), box 64 features x 1 row,
+    // 128-byte swizzle: the producer's tile::gather4 loads read 4 rows of it per instruction
+    CUtensorMap tmap;
     const int32_t *ptr, *idx, *order;
     const float *val;
     const __nv_bfloat16 *Ybf;  // (n_opp + 1) x fst, row n_opp all zero
@@ -95,15 +104,18 @@ inline Geometry geometry(int f, int solver) {
     const int acc_cols = g.ng + 16;
     g.acc_stride = acc_cols <= 128 ? 128 : 256;
     g.nbuf = acc_cols <= 128 ? 4 : 2;
-    // CG / LU groups double-buffer their accumulator; a Cholesky group copies its Gram to shared
-    // memory at once, so it takes one buffer and twice as many groups share the SM
+    // Accumulators rotate over the groups (group g takes rows g, g + nepi, ...; row k lands in
+    // buffer k % nbuf).  CG and LU read their row out of TMEM into registers at once and release
+    // the buffer, so the MMA fills the next row while they solve; their register-resident rows
+    // (168 registers a thread) allow two groups per SM.  A Cholesky group keeps its buffer until
+    // refinement has re-read A, and its factor lives in shared memory: one group per buffer.
     g.nepi = solver == SOLVER_CHOL ? g.nbuf : g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
     g.nthreads = 64 + 128 * g.nepi;
     const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
-    bytes += sizeof(int32_t) * ns * KC;                              // gathered column ids
+    bytes += MRING_BYTES;                                            // metadata ring
     bytes += 1024;                                                   // metas, barriers, scalars
     g.smem = bytes + 1024;                                           // 1024-B alignment slack
     return g;
@@ -157,18 +169,38 @@ __device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, vo
 __device__ __forceinline__ void fence_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+// 4-byte asynchronous global -> shared copy (the ratings of a stage have no alignment).
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// Arrive on `bar` once every cp.async this thread issued so far has landed (pending count is not
-// raised: the arrival counts against the barrier's expected count).
-__device__ __forceinline__ void cp_arrive_noinc(uint32_t bar) {
-    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
-}
 template <int N>
 __device__ __forceinline__ void cp_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Arrive on `bar` and add `bytes` to the transaction count its current phase waits for.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+// TMA gather: rows r0..r3 of the 2-D tensor map, features x .. x+63 (x * 2 bytes a multiple of
+// 16), land as four consecutive 128-byte rows at dst (128-byte swizzle by address); the bytes
+// count against `bar`'s transaction count.  `policy` is an L2 cache policy: the gathered table is
+// re-read by every SM for the whole half-sweep.
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap *tmap, int x, int r0,
+                                            int r1, int r2, int r3, uint32_t bar,
+                                            uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        ".L2::cache_hint [%0], [%1, {%2, %3, %4, %5, %6}], [%7], %8;" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(bar),
+        "l"(policy)
+        : "memory");
+}
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
 }
 __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -259,9 +291,11 @@ __device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *
 __device__ __forceinline__ int lane_of(int i) { return i & 31; }
 
 // The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
+// Returns true when it released the accumulator itself (arrived on `release` once every thread
+// of the group had read its row out of TMEM); otherwise the caller releases it afterwards.
 template <int FP, int SOLVER>
-__device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
-                          float *gsm, const GroupSync &gs) {
+__device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
+                          float *gsm, const GroupSync &gs, uint32_t release) {
     float *Ls = gsm;
     float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
@@ -280,6 +314,7 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     int slot = 0;
     float xi = 0.f;
     bool good = true;
+    bool released = false;
     if constexpr (SOLVER == SOLVER_CHOL) {
         // Cholesky (+ refinement against the TMEM copy of A).  The regularised Gram's lower
         // triangle moves to the packed shared-memory layout in 32-column chunks (a warp reads
@@ -384,6 +419,11 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 #pragma unroll
         for (int j = 0; j < FP; ++j)
             if (j == i) a[j] = i < f ? a[j] + reg : 1.f;  // identity on the padded rows
+        // the row is in registers: hand the accumulator back to the MMA issuer now
+        tc_fence_before();
+        gs.sync();
+        if (et == 0) mbar_arrive(release);
+        released = true;
 
         if constexpr (SOLVER == SOLVER_CG) {
             xi = cg_reg<FP>(a, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
@@ -414,18 +454,21 @@ __device__ void solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     } else if (i < f) {
         xo[i] = xi;
     }
+    return released;
 }
 
 template <int FP, int SOLVER>
 __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
-    sweep_tc_kernel(const Params p) {
+    sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
     float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
-    int32_t *scol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * p.nepi);
-    Meta *smeta = (Meta *)(((uintptr_t)(scol + NSTAGE * KC) + 15) & ~(uintptr_t)15);
+    int32_t *mcol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * p.nepi);  // [MR][KC]
+    float *mval = reinterpret_cast<float *>(mcol + MR * KC);                            // [MR][KC]
+    Meta *mmeta = reinterpret_cast<Meta *>(mval + MR * KC);                             // [MR]
+    Meta *smeta = mmeta + MR;
     Meta *ameta = smeta + NSTAGE;
     uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
     uint64_t *full = bars, *empty = bars + NSTAGE;
@@ -444,7 +487,7 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
-            mbar_init(smem_u32(&full[s]), 33);  // 32 producer lanes' copies + lane 0's arrive
+            mbar_init(smem_u32(&full[s]), 1);  // lane 0's arrive.expect_tx + the TMA bytes
             mbar_init(smem_u32(&empty[s]), 1);
         }
         for (int b = 0; b < MAX_NBUF; ++b) {
@@ -471,146 +514,139 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
 
     if (warp == 0) {
         // ------------------------------------------------------------------ producer
-        // Rows come in chunks from the atomic counter: one at a time among the first `head`
-        // slots (the heaviest rows, for balance), CH at a time after that.  Lane j of a chunk
-        // holds its row j's (row, beg, end); the next chunk is grabbed and its row ids loaded
-        // while the current one streams, and each stage's column ids and ratings are loaded one
-        // stage ahead, so the gather never waits on a dependent metadata load.
+        // Two cursors walk the same sequence of stages (KC ratings of one row each).  The
+        // look-ahead cursor issues a stage's column ids and ratings as 4-byte cp.async into the
+        // metadata ring MD stages ahead, with its Meta; the gather side then only waits for that
+        // cp.async group, writes the rating tile and issues one tile::gather4 per lane (4 ratings
+        // x 64 features).  Rows come in chunks from the atomic counter (one at a time among the
+        // first `head` slots, the heaviest rows, then CH at a time), pipelined two chunks ahead
+        // so the dependent order[] -> ptr[] loads have landed when a chunk starts.
         constexpr int CH = 8;
-        const int nchunk = p.fst / 8;
-        const int kq = 32 / nchunk, kr = 32 % nchunk;        // (k, c) step per 32 lanes
-        const int k_l = lane / nchunk, c_l = lane % nchunk;
+        const int natoms = p.fst > 64 ? 2 : 1;               // 64-feature atoms per rating
+        const int gq = lane & 15, ga = lane >> 4;            // this lane's 4-rating quad, atom
+        const uint64_t keep = l2_evict_last_policy();
         const int head = 4 * (int)gridDim.x;
-        const char *ybytes = reinterpret_cast<const char *>(p.Ybf);
-        uint32_t it = 0;        // stage counter
-        bool ok = true;
         int grab_size = 1;
-        // A stage completes when every lane's copies have landed (cp.async arrive, no waiting
-        // here) and lane 0 has published its metadata and rating tile (ordinary arrive after a
-        // proxy fence, so the tensor core sees the generic stores).
-        auto signal_stage = [&](int s) {
-            cp_arrive_noinc(smem_u32(&full[s]));
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&full[s]));
-        };
-        auto grab = [&](int &cbase, int &ccnt) {
+        auto grab = [&](int &cb, int &cc) {
             int b = 0;
             if (lane == 0) b = atomicAdd(p.work, grab_size);
             b = __shfl_sync(0xffffffffu, b, 0);
-            cbase = b;
-            ccnt = max(0, min(grab_size, p.nrows - b));
+            cb = b;
+            cc = max(0, min(grab_size, p.nrows - b));
             if (b + grab_size >= head) grab_size = CH;
         };
-        // current chunk
-        int cbase, ccnt;
-        grab(cbase, ccnt);
-        int crow = lane < ccnt ? p.order[cbase + lane] : 0;
-        int cbeg = lane < ccnt ? p.ptr[crow] : 0;
-        int cend = lane < ccnt ? p.ptr[crow + 1] : 0;
-        // stage cursor (j = row of the chunk, base = first rating of the stage) + prefetch
-        auto stage_load = [&](int j, int base, int &c0, int &c1, float &v0, float &v1) {
-            const int e = __shfl_sync(0xffffffffu, cend, j);
-            const int cnt = min(KC, e - base);
-            c0 = lane < cnt ? p.idx[base + lane] : p.zero_row;
-            c1 = lane + 32 < cnt ? p.idx[base + lane + 32] : p.zero_row;
-            v0 = lane < cnt ? p.val[base + lane] : 0.f;
-            v1 = lane + 32 < cnt ? p.val[base + lane + 32] : 0.f;
-        };
-        while (ok && ccnt > 0) {
-            // grab the next chunk and start loading its row ids while this one streams
-            int nbase, ncnt;
-            grab(nbase, ncnt);
-            const int nrow = lane < ncnt ? p.order[nbase + lane] : 0;
-            // stage cursors t (j, base), t+1 (j1, b1) with their column ids / ratings in flight;
-            // t+2 is loaded while t is issued
-            auto advance = [&](int jj, int bb, int &jo, int &bo) {
-                const int e = __shfl_sync(0xffffffffu, cend, jj);
-                jo = jj;
-                bo = bb + KC;
-                if (bo >= e) {
-                    ++jo;
-                    bo = jo < ccnt ? __shfl_sync(0xffffffffu, cbeg, jo < ccnt ? jo : 0) : 0;
-                }
-            };
-            int j = 0;
-            int base = __shfl_sync(0xffffffffu, cbeg, 0);
-            int c0, c1;
-            float v0, v1;
-            stage_load(0, base, c0, c1, v0, v1);
-            int j1, b1;
-            advance(j, base, j1, b1);
-            int d0 = 0, d1 = 0;
-            float w0 = 0.f, w1 = 0.f;
-            if (j1 < ccnt) stage_load(j1, b1, d0, d1, w0, w1);
-            while (j < ccnt) {
-                const int row = __shfl_sync(0xffffffffu, crow, j);
-                const int beg = __shfl_sync(0xffffffffu, cbeg, j);
-                const int end = __shfl_sync(0xffffffffu, cend, j);
-                const int cnt = min(KC, end - base);
-                int j2 = ccnt, b2 = 0;
-                if (j1 < ccnt) advance(j1, b1, j2, b2);
-                int pc0 = 0, pc1 = 0;
-                float pv0 = 0.f, pv1 = 0.f;
-                if (j2 < ccnt) stage_load(j2, b2, pc0, pc1, pv0, pv1);
-
-                const int s = it % NSTAGE;
-                if (it >= NSTAGE &&
-                    !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
-                    ok = false;
-                    break;
-                }
-                uint8_t *tile = ring + s * STAGE_BYTES;
-                __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
-                scol[s * KC + lane] = c0;
-                scol[s * KC + lane + 32] = c1;
-                rt[lane] = __float2bfloat16_rn(v0);
-                rt[lane + 32] = __float2bfloat16_rn(v1);
-                __syncwarp();
-                const int lim = ((cnt + 15) & ~15) * nchunk;
-                const uint32_t tile_s = smem_u32(tile);
-                int k = k_l, c = c_l;
-                for (int e = lane; e < lim; e += 32) {
-                    const int col = scol[s * KC + k];
-                    const uint32_t dst = tile_s + (c >> 3) * ATOM_STRIDE + (k >> 3) * ATOM_BYTES +
-                                         (k & 7) * 128 + (((c & 7) ^ (k & 7)) << 4);
-                    cp_async16(dst, ybytes + ((size_t)col * p.fst + (size_t)c * 8) * 2);
-                    k += kq;
-                    c += kr;
-                    if (c >= nchunk) {
-                        c -= nchunk;
-                        ++k;
-                    }
-                }
-                if (lane == 0) {
-                    Meta m;
-                    m.row = row;
-                    m.cnt = cnt;
-                    m.flags = (base == beg ? 1 : 0) | (base + KC >= end ? 2 : 0);
-                    m.nu = end - beg;
-                    smeta[s] = m;
-                }
-                signal_stage(s);
-                ++it;
-                j = j1;
-                base = b1;
-                c0 = d0;
-                c1 = d1;
-                v0 = w0;
-                v1 = w1;
-                j1 = j2;
-                b1 = b2;
-                d0 = pc0;
-                d1 = pc1;
-                w0 = pv0;
-                w1 = pv1;
-            }
-            // switch to the next chunk
-            cbase = nbase;
-            ccnt = ncnt;
-            crow = nrow;
+        // chunk pipeline: current (row, beg, end in lane j), next (row, beg, end), next-next (row)
+        int ccnt, crow, cbeg, cend, n1cnt, n1row, n1beg, n1end, n2cnt, n2row;
+        {
+            int cb;
+            grab(cb, ccnt);
+            crow = lane < ccnt ? p.order[cb + lane] : 0;
+            grab(cb, n1cnt);
+            n1row = lane < n1cnt ? p.order[cb + lane] : 0;
+            grab(cb, n2cnt);
+            n2row = lane < n2cnt ? p.order[cb + lane] : 0;
             cbeg = lane < ccnt ? p.ptr[crow] : 0;
             cend = lane < ccnt ? p.ptr[crow + 1] : 0;
+            n1beg = lane < n1cnt ? p.ptr[n1row] : 0;
+            n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
+        }
+        int aj = 0;                                          // look-ahead cursor: row of chunk
+        int abase = __shfl_sync(0xffffffffu, cbeg, 0);       // and first rating of its stage
+        uint32_t gen = 0;                                    // stages issued by the look-ahead
+        // issue the metadata of stage `gen`; false once no rows are left
+        auto generate = [&]() -> bool {
+            while (aj >= ccnt) {
+                if (ccnt <= 0) return false;
+                ccnt = n1cnt; crow = n1row; cbeg = n1beg; cend = n1end;
+                n1cnt = n2cnt; n1row = n2row;
+                n1beg = lane < n1cnt ? p.ptr[n1row] : 0;     // n2's row ids landed a chunk ago
+                n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
+                int cb;
+                grab(cb, n2cnt);
+                n2row = lane < n2cnt ? p.order[cb + lane] : 0;
+                aj = 0;
+                if (ccnt <= 0) return false;
+                abase = __shfl_sync(0xffffffffu, cbeg, 0);
+            }
+            const int row = __shfl_sync(0xffffffffu, crow, aj);
+            const int beg = __shfl_sync(0xffffffffu, cbeg, aj);
+            const int end = __shfl_sync(0xffffffffu, cend, aj);
+            const int cnt = min(KC, end - abase);
+            const int slot = (int)(gen % MR);
+            int32_t *mc = mcol + slot * KC;
+            float *mv = mval + slot * KC;
+#pragma unroll
+            for (int h = 0; h < KC; h += 32) {
+                if (lane + h < cnt) {
+                    cp_async4(smem_u32(mc + lane + h), p.idx + abase + lane + h);
+                    cp_async4(smem_u32(mv + lane + h), p.val + abase + lane + h);
+                } else {
+                    mc[lane + h] = p.zero_row;   // the ragged tail gathers the all-zero row
+                    mv[lane + h] = 0.f;
+                }
+            }
+            cp_commit();
+            if (lane == 0) {
+                Meta m;
+                m.row = row;
+                m.cnt = cnt;
+                m.flags = (abase == beg ? 1 : 0) | (abase + KC >= end ? 2 : 0);
+                m.nu = end - beg;
+                mmeta[slot] = m;
+            }
+            abase += KC;
+            if (abase >= end) {
+                ++aj;
+                abase = aj < ccnt ? __shfl_sync(0xffffffffu, cbeg, aj < ccnt ? aj : 0) : 0;
+            }
+            ++gen;
+            return true;
+        };
+        bool more = true;
+        for (int k = 0; k < MD && more; ++k) more = generate();
+        uint32_t it = 0;        // stages gathered
+        bool ok = true;
+        while (it < gen) {
+            // stage it's metadata group: at most gen - it - 1 younger groups may stay pending
+            if (gen - it - 1 >= (uint32_t)(MD - 1))
+                cp_wait<MD - 1>();
+            else
+                cp_wait<0>();
+            __syncwarp();
+            const int s = it % NSTAGE;
+            if (it >= NSTAGE &&
+                !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
+                ok = false;
+                break;
+            }
+            const int slot = (int)(it % MR);
+            const Meta m = mmeta[slot];
+            uint8_t *tile = ring + s * STAGE_BYTES;
+            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
+            rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
+            rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
+            // the rating tile is a generic store: visible to the tensor core (async proxy) before
+            // the stage is published
+            fence_async_smem();
+            __syncwarp();
+            // the MMA reads ratings [0, 16 nk): gather 4 nk quads (the ragged tail's column ids
+            // point at the zero row), 512 bytes per quad and atom
+            const int nq = ((m.cnt + 15) >> 4) * 4;
+            if (lane == 0) {
+                smeta[s] = m;
+                mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
+            }
+            __syncwarp();
+            if (gq < nq && ga < natoms) {
+                const int32_t *q = mcol + slot * KC + 4 * gq;
+                const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE + (gq >> 1) * ATOM_BYTES +
+                                     (gq & 1) * 512;
+                tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3], smem_u32(&full[s]),
+                            keep);
+            }
+            __syncwarp();   // every lane has read the slot before the look-ahead refills it
+            ++it;
+            if (more) more = generate();
         }
         if (ok) {  // the end marker: one stage with row = -1
             const int s = it % NSTAGE;
@@ -625,13 +661,23 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
                     m.flags = 3;
                     m.nu = 0;
                     smeta[s] = m;
+                    mbar_arrive(smem_u32(&full[s]));
                 }
-                signal_stage(s);
+                __syncwarp();
                 ++it;
             }
         }
-        cp_commit();
-        cp_wait<0>();  // nothing of this warp is in flight when the CTA tears down
+        // nothing of this warp may be in flight when the CTA tears down: the metadata copies,
+        // and the last NSTAGE stages' gathers (their full barriers complete once the bytes have
+        // landed; bounded wait, also on abort; no slot was reused after them, so each parity is
+        // unambiguous)
+        cp_wait<0>();
+        if (lane == 0) {
+            const uint32_t from = it > (uint32_t)NSTAGE ? it - NSTAGE : 0;
+            for (uint32_t u = from; u < it; ++u)
+                mbar_wait(smem_u32(&full[u % NSTAGE]), (u / NSTAGE) & 1, nullptr);
+        }
+        __syncwarp();
         if (!ok) {
             *abort = 1;
             if (lane == 0) atomicAdd(&p.flags[2], 1);
@@ -682,7 +728,8 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
                 mma_commit(smem_u32(&empty[s]));
                 if (m.flags & 2) {
                     ameta[buf] = m;
-                    if (m.nu > 0) mma_commit(smem_u32(&acc_full[buf]));
+                    // committed for empty rows too, so buffer b's phase count is its use count
+                    mma_commit(smem_u32(&acc_full[buf]));
                     mbar_arrive(smem_u32(&acc_meta[buf]));
                     ++acc_it;
                 }
@@ -706,7 +753,6 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         const GroupSync gs{1 + g};
         float *gsm = gscratch + GroupLayout<FP, SOLVER>::floats * g;
         volatile int *okflag = grp_ok + g;
-        uint32_t fullcnt[2] = {0, 0};
         bool ok = true;
         auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
             if (et == 0) *okflag = mbar_wait(bar, parity, abort) ? 1 : 0;
@@ -718,22 +764,24 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         for (uint32_t acc_it = g;; acc_it += p.nepi) {
             const uint32_t buf = acc_it % nbuf;
             const uint32_t use = acc_it / nbuf;
-            const int lb = (int)(buf / p.nepi);      // 0/1: this group's two buffers
             if (!group_wait(smem_u32(&acc_meta[buf]), use & 1)) { ok = false; break; }
             const Meta m = ameta[buf];
             if (m.row < 0) break;
+            if (!group_wait(smem_u32(&acc_full[buf]), use & 1)) { ok = false; break; }
+            tc_fence_after();
+            bool released = false;
             if (m.nu > 0) {
-                if (!group_wait(smem_u32(&acc_full[buf]), fullcnt[lb] & 1)) { ok = false; break; }
-                ++fullcnt[lb];
-                tc_fence_after();
                 const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
-                solve_row<FP, SOLVER>(p, m, tb, i, et, g, gsm, gs);
+                released = solve_row<FP, SOLVER>(p, m, tb, i, et, g, gsm, gs,
+                                                 smem_u32(&acc_empty[buf]));
             } else if (i < p.f) {
                 p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
             }
-            tc_fence_before();
-            gs.sync();
-            if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
+            if (!released) {
+                tc_fence_before();
+                gs.sync();
+                if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
+            }
         }
         if (!ok) {
             *abort = 1;

@@ -93,18 +93,28 @@ def test_auto_training_reaches_fp32_cholesky_rmse(precision):
     (ca.PRECISION.FP32, ca.SOLVE_TYPE.CUMF_ALS_CG_FP32),
 ])
 def test_graph_epochs_match_eager_bits(precision, solve):
-    """Rows are independent and each row's arithmetic has a fixed order, so a replayed epoch must
-    reproduce the eager epoch bit for bit (whichever SM takes which row)."""
+    """Rows are independent and each row's arithmetic has a fixed order, so an epoch replayed from
+    the captured graph must reproduce the same epoch launched eagerly (half_sweep U, then V) bit
+    for bit, from the same factors and with the same plan (one handle: under AUTO the plan comes
+    from timings, so two handles may tune differently)."""
     tr, te, info = workload2()
-    out = []
-    for use_graph in (0, 1):
-        with model(tr, te, info, solve, precision, use_graph=use_graph) as mdl:
-            mdl.init_factors()
-            for _ in range(5):
-                mdl.iterate(1)
-            out.append(mdl.get_factors())
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1])
+    with model(tr, te, info, solve, precision, use_graph=1) as mdl:
+        mdl.init_factors()
+        mdl.iterate(4)                      # plan final (tuned under AUTO), epoch captured
+        U0, V0 = mdl.get_factors()
+        mdl.iterate(1)                      # replayed
+        Ug, Vg = mdl.get_factors()
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(0)                   # eager
+        mdl.half_sweep(1)
+        Ue, Ve = mdl.get_factors()
+    assert np.array_equal(Ug, Ue) and np.array_equal(Vg, Ve)
+    if solve != ca.SOLVE_TYPE.AUTO:         # a fixed plan: a handle without graphs agrees too
+        with model(tr, te, info, solve, precision, use_graph=0) as mdl:
+            mdl.set_factors(U0, V0)
+            mdl.iterate(1)
+            Un, Vn = mdl.get_factors()
+        assert np.array_equal(Ug, Un) and np.array_equal(Vg, Vn)
 
 
 def test_graph_survives_value_update_and_reload():
