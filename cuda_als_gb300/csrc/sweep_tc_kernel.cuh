@@ -33,6 +33,9 @@ constexpr int MAX_NBUF = 4;
 // stages ahead of its gathers (MR slots, MR > MD), so their HBM latency never stalls the gathers.
 constexpr int MD = 12;
 constexpr int MR = 16;
+// Extra warps that issue TMA gathers: one warp issues a tile::gather4 only every ~90 cycles, so the
+// stages are spread round-robin over the producer and NHELP gather warps.
+constexpr int NHELP = 2;
 constexpr int MRING_BYTES = MR * KC * 8 + MR * 16;   // column ids, ratings, Meta per slot
 enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2 };
 constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
@@ -111,11 +114,12 @@ inline Geometry geometry(int f, int solver) {
     // refinement has re-read A, and its factor lives in shared memory: one group per buffer.
     g.nepi = solver == SOLVER_CHOL ? g.nbuf : g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
-    g.nthreads = 64 + 128 * g.nepi;
+    g.nthreads = 64 + 128 * g.nepi + 32 * NHELP;
     const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
     bytes += MRING_BYTES;                                            // metadata ring
+    bytes += sizeof(int32_t) * ns * KC;                              // column ids per stage
     bytes += 1024;                                                   // metas, barriers, scalars
     g.smem = bytes + 1024;                                           // 1024-B alignment slack
     return g;
@@ -458,7 +462,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 }
 
 template <int FP, int SOLVER>
-__global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
+__global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 + 32 * NHELP : 320 + 32 * NHELP, 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
     extern __shared__ uint8_t smem_raw[];
@@ -468,7 +472,8 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
     int32_t *mcol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * p.nepi);  // [MR][KC]
     float *mval = reinterpret_cast<float *>(mcol + MR * KC);                            // [MR][KC]
     Meta *mmeta = reinterpret_cast<Meta *>(mval + MR * KC);                             // [MR]
-    Meta *smeta = mmeta + MR;
+    int32_t *scol = reinterpret_cast<int32_t *>(mmeta + MR);           // [NSTAGE][KC] per stage
+    Meta *smeta = reinterpret_cast<Meta *>(scol + NSTAGE * KC);
     Meta *ameta = smeta + NSTAGE;
     uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
     uint64_t *full = bars, *empty = bars + NSTAGE;
@@ -478,6 +483,8 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
     uint32_t *tmem_slot = (uint32_t *)(drain + 1);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
     volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
+    volatile int *pub = grp_ok + MAX_NBUF;  // stages the producer has set up for the gather warps
+    volatile int *fin = pub + 1;            // the producer has set up its last stage
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nbuf = p.nbuf;
@@ -487,7 +494,9 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
-            mbar_init(smem_u32(&full[s]), 1);  // lane 0's arrive.expect_tx + the TMA bytes
+            // the producer's arrive.expect_tx, the gathering warp's arrive once it has read the
+            // stage's column ids and issued its gathers, and the TMA bytes
+            mbar_init(smem_u32(&full[s]), 2);
             mbar_init(smem_u32(&empty[s]), 1);
         }
         for (int b = 0; b < MAX_NBUF; ++b) {
@@ -497,6 +506,8 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         }
         mbar_init(smem_u32(drain), 1);
         *abort = 0;
+        *pub = 0;
+        *fin = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_async_smem();
@@ -625,6 +636,10 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
             __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
             rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
             rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
+            // the stage's column ids move to its own array: a gather warp may read them after the
+            // look-ahead has refilled the metadata slot
+            scol[s * KC + lane] = mcol[slot * KC + lane];
+            scol[s * KC + lane + 32] = mcol[slot * KC + lane + 32];
             // the rating tile is a generic store: visible to the tensor core (async proxy) before
             // the stage is published
             fence_async_smem();
@@ -637,16 +652,28 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
                 mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
             }
             __syncwarp();
-            if (gq < nq && ga < natoms) {
-                const int32_t *q = mcol + slot * KC + 4 * gq;
-                const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE + (gq >> 1) * ATOM_BYTES +
-                                     (gq & 1) * 512;
-                tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3], smem_u32(&full[s]),
-                            keep);
+            if (it % (NHELP + 1) == 0) {  // this warp's share of the stages
+                if (gq < nq && ga < natoms) {
+                    const int32_t *q = scol + s * KC + 4 * gq;
+                    const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE +
+                                         (gq >> 1) * ATOM_BYTES + (gq & 1) * 512;
+                    tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3],
+                                smem_u32(&full[s]), keep);
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&full[s]));
+            }
+            if (lane == 0) {  // publish the stage (its column ids, Meta and byte count are set)
+                __threadfence_block();
+                *pub = (int)(it + 1);
             }
             __syncwarp();   // every lane has read the slot before the look-ahead refills it
             ++it;
             if (more) more = generate();
+        }
+        if (lane == 0) {  // no further stages for the gather warps
+            __threadfence_block();
+            *fin = 1;
         }
         if (ok) {  // the end marker: one stage with row = -1
             const int s = it % NSTAGE;
@@ -661,6 +688,7 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
                     m.flags = 3;
                     m.nu = 0;
                     smeta[s] = m;
+                    mbar_arrive(smem_u32(&full[s]));
                     mbar_arrive(smem_u32(&full[s]));
                 }
                 __syncwarp();
@@ -786,6 +814,50 @@ __global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 : 320, 1)
         if (!ok) {
             *abort = 1;
             if (et == 0) atomicAdd(&p.flags[2], 1);
+        }
+    } else {
+        // ------------------------------------------------------------------ gather warps
+        // Warp h takes the stages t = h + 1, h + 1 + (NHELP + 1), ... once the producer has
+        // published them: it reads the stage's column ids, issues its tile::gather4 loads and
+        // arrives on the stage's full barrier.  It runs until the producer has finished and every
+        // published stage of its share is issued (also after an abort, so every full barrier the
+        // producer set up completes and the final drain ends).
+        const int h = warp - (2 + 4 * p.nepi);
+        const int natoms = p.fst > 64 ? 2 : 1;
+        const int gq = lane & 15, ga = lane >> 4;
+        const uint64_t keep = l2_evict_last_policy();
+        bool ok = true;
+        for (uint32_t t = (uint32_t)h + 1;; t += NHELP + 1) {
+            int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out
+            if (lane == 0) {
+                const unsigned long long t0 = now_ns();
+                for (uint32_t k = 0;; ++k) {
+                    if ((uint32_t)*pub > t) { go = 1; break; }
+                    if (*fin) { go = (uint32_t)*pub > t ? 1 : 0; break; }
+                    if ((k & 255) == 255 && now_ns() - t0 > WAIT_NS) { go = -1; break; }
+                }
+                __threadfence_block();
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (go <= 0) {
+                ok = go == 0;
+                break;
+            }
+            const int s = t % NSTAGE;
+            const int nq = ((smeta[s].cnt + 15) >> 4) * 4;
+            if (gq < nq && ga < natoms) {
+                const int32_t *q = scol + s * KC + 4 * gq;
+                const uint32_t dst = smem_u32(ring + s * STAGE_BYTES) + ga * ATOM_STRIDE +
+                                     (gq >> 1) * ATOM_BYTES + (gq & 1) * 512;
+                tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3], smem_u32(&full[s]),
+                            keep);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[s]));
+        }
+        if (!ok) {
+            *abort = 1;
+            if (lane == 0) atomicAdd(&p.flags[2], 1);
         }
     }
 
