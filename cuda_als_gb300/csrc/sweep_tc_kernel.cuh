@@ -268,6 +268,69 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// TMEM -> registers: the Gram row's FP columns and b (column bcol, one more 1-column load) with
+// one wait::ld per block of at most 64 columns (larger blocks put the row in local memory);
+// loads and their wait share one asm block, so no output is read before it arrived.
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float (&a)[32], float &b) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%32}, [%34];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(b)
+        : "r"(taddr + 0u), "r"(taddr + bcol)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float (&a)[64], float &b) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%65];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%66];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%64}, [%67];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(a[32]), "=f"(a[33]), "=f"(a[34]), "=f"(a[35]), "=f"(a[36]), "=f"(a[37]), "=f"(a[38]), "=f"(a[39]), "=f"(a[40]), "=f"(a[41]), "=f"(a[42]), "=f"(a[43]), "=f"(a[44]), "=f"(a[45]), "=f"(a[46]), "=f"(a[47]), "=f"(a[48]), "=f"(a[49]), "=f"(a[50]), "=f"(a[51]), "=f"(a[52]), "=f"(a[53]), "=f"(a[54]), "=f"(a[55]), "=f"(a[56]), "=f"(a[57]), "=f"(a[58]), "=f"(a[59]), "=f"(a[60]), "=f"(a[61]), "=f"(a[62]), "=f"(a[63]), "=f"(b)
+        : "r"(taddr + 0u), "r"(taddr + 32u), "r"(taddr + bcol)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float (&a)[112], float &b) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(a[32]), "=f"(a[33]), "=f"(a[34]), "=f"(a[35]), "=f"(a[36]), "=f"(a[37]), "=f"(a[38]), "=f"(a[39]), "=f"(a[40]), "=f"(a[41]), "=f"(a[42]), "=f"(a[43]), "=f"(a[44]), "=f"(a[45]), "=f"(a[46]), "=f"(a[47]), "=f"(a[48]), "=f"(a[49]), "=f"(a[50]), "=f"(a[51]), "=f"(a[52]), "=f"(a[53]), "=f"(a[54]), "=f"(a[55]), "=f"(a[56]), "=f"(a[57]), "=f"(a[58]), "=f"(a[59]), "=f"(a[60]), "=f"(a[61]), "=f"(a[62]), "=f"(a[63])
+        : "r"(taddr + 0u), "r"(taddr + 32u)
+        : "memory");
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%48}, [%51];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[64]), "=f"(a[65]), "=f"(a[66]), "=f"(a[67]), "=f"(a[68]), "=f"(a[69]), "=f"(a[70]), "=f"(a[71]), "=f"(a[72]), "=f"(a[73]), "=f"(a[74]), "=f"(a[75]), "=f"(a[76]), "=f"(a[77]), "=f"(a[78]), "=f"(a[79]), "=f"(a[80]), "=f"(a[81]), "=f"(a[82]), "=f"(a[83]), "=f"(a[84]), "=f"(a[85]), "=f"(a[86]), "=f"(a[87]), "=f"(a[88]), "=f"(a[89]), "=f"(a[90]), "=f"(a[91]), "=f"(a[92]), "=f"(a[93]), "=f"(a[94]), "=f"(a[95]), "=f"(a[96]), "=f"(a[97]), "=f"(a[98]), "=f"(a[99]), "=f"(a[100]), "=f"(a[101]), "=f"(a[102]), "=f"(a[103]), "=f"(a[104]), "=f"(a[105]), "=f"(a[106]), "=f"(a[107]), "=f"(a[108]), "=f"(a[109]), "=f"(a[110]), "=f"(a[111]), "=f"(b)
+        : "r"(taddr + 64u), "r"(taddr + 96u), "r"(taddr + bcol)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float (&a)[128], float &b) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%65];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(a[32]), "=f"(a[33]), "=f"(a[34]), "=f"(a[35]), "=f"(a[36]), "=f"(a[37]), "=f"(a[38]), "=f"(a[39]), "=f"(a[40]), "=f"(a[41]), "=f"(a[42]), "=f"(a[43]), "=f"(a[44]), "=f"(a[45]), "=f"(a[46]), "=f"(a[47]), "=f"(a[48]), "=f"(a[49]), "=f"(a[50]), "=f"(a[51]), "=f"(a[52]), "=f"(a[53]), "=f"(a[54]), "=f"(a[55]), "=f"(a[56]), "=f"(a[57]), "=f"(a[58]), "=f"(a[59]), "=f"(a[60]), "=f"(a[61]), "=f"(a[62]), "=f"(a[63])
+        : "r"(taddr + 0u), "r"(taddr + 32u)
+        : "memory");
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%65];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%66];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%64}, [%67];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[64]), "=f"(a[65]), "=f"(a[66]), "=f"(a[67]), "=f"(a[68]), "=f"(a[69]), "=f"(a[70]), "=f"(a[71]), "=f"(a[72]), "=f"(a[73]), "=f"(a[74]), "=f"(a[75]), "=f"(a[76]), "=f"(a[77]), "=f"(a[78]), "=f"(a[79]), "=f"(a[80]), "=f"(a[81]), "=f"(a[82]), "=f"(a[83]), "=f"(a[84]), "=f"(a[85]), "=f"(a[86]), "=f"(a[87]), "=f"(a[88]), "=f"(a[89]), "=f"(a[90]), "=f"(a[91]), "=f"(a[92]), "=f"(a[93]), "=f"(a[94]), "=f"(a[95]), "=f"(a[96]), "=f"(a[97]), "=f"(a[98]), "=f"(a[99]), "=f"(a[100]), "=f"(a[101]), "=f"(a[102]), "=f"(a[103]), "=f"(a[104]), "=f"(a[105]), "=f"(a[106]), "=f"(a[107]), "=f"(a[108]), "=f"(a[109]), "=f"(a[110]), "=f"(a[111]), "=f"(a[112]), "=f"(a[113]), "=f"(a[114]), "=f"(a[115]), "=f"(a[116]), "=f"(a[117]), "=f"(a[118]), "=f"(a[119]), "=f"(a[120]), "=f"(a[121]), "=f"(a[122]), "=f"(a[123]), "=f"(a[124]), "=f"(a[125]), "=f"(a[126]), "=f"(a[127]), "=f"(b)
+        : "r"(taddr + 64u), "r"(taddr + 96u), "r"(taddr + bcol)
+        : "memory");
+}
+
 // ------------------------------------------------------------------------------------- kernels
 
 // sum_j D[i][j] x_j re-read from TMEM in 16-column chunks (FP64 products and sums when WIDE)
@@ -309,8 +372,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     float *xo = p.X + (int64_t)m.row * f;
     const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
 
-    float bi;
-    {
+    float bi = 0.f;
+    if constexpr (SOLVER == SOLVER_CHOL) {
         float v[16];
         tmem_ld16(tb + p.ng, v);
         bi = i < f ? v[0] : 0.f;
@@ -403,22 +466,14 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // the CG warm start is a global load: issue it before the TMEM reads so they overlap
         const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
+        // the Gram row (columns < ng) and b (column ng) in one or two TMEM round trips
         float a[FP];
+        {
+            float b;
+            tmem_ld_row(tb, (uint32_t)p.ng, a, b);
 #pragma unroll
-        for (int c = 0; c < FP; c += 32) {
-            if (c + 32 <= FP && c + 32 <= p.ng) {
-                tmem_ld32(tb + c, &a[c]);
-            } else {
-#pragma unroll
-                for (int h = 0; h < 32 && c + h < FP; h += 16) {
-                    if (c + h < p.ng) {
-                        tmem_ld16(tb + c + h, &a[c + h]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) a[c + h + j] = 0.f;
-                    }
-                }
-            }
+            for (int j = 0; j < FP; ++j) a[j] = j < p.ng ? a[j] : 0.f;
+            bi = i < f ? b : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < FP; ++j)
