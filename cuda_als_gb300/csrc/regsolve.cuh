@@ -92,6 +92,62 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
     return xi;
 }
 
+// CG as cg_reg with each thread's row split: columns [0, R) in registers (ar), [R, FP) in shared
+// memory (srow: the thread's own FP - R floats, 16-byte aligned, rows an odd number of float4
+// apart so a quarter warp's float4 loads hit distinct banks).  Frees the registers that let more
+// solver groups share an SM.
+template <int FP, int R>
+__device__ __forceinline__ float dot_split(const float (&ar)[R], const float *srow,
+                                           const float *sv) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+    for (int j = 0; j < R; j += 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(sv + j);
+        s0 = fmaf(ar[j], v.x, s0);
+        s1 = fmaf(ar[j + 1], v.y, s1);
+        s2 = fmaf(ar[j + 2], v.z, s2);
+        s3 = fmaf(ar[j + 3], v.w, s3);
+    }
+#pragma unroll
+    for (int j = 0; j < FP - R; j += 4) {
+        const float4 a = *reinterpret_cast<const float4 *>(srow + j);
+        const float4 v = *reinterpret_cast<const float4 *>(sv + R + j);
+        s0 = fmaf(a.x, v.x, s0);
+        s1 = fmaf(a.y, v.y, s1);
+        s2 = fmaf(a.z, v.z, s2);
+        s3 = fmaf(a.w, v.w, s3);
+    }
+    return (s0 + s1) + (s2 + s3);
+}
+
+template <int FP, int R>
+__device__ float cg_split(const float (&ar)[R], const float *srow, float bi, float xi, int i,
+                          float *sv, float *red, int iters, float tol, const GroupSync &gs) {
+    int slot = 0;
+    const bool live = i < FP;
+    if (live) sv[i] = xi;
+    gs.sync();
+    float r = bi - dot_split<FP, R>(ar, srow, sv);
+    float p = r;
+    float rsold = gsum128(r * r, red, slot, gs);
+    for (int it = 0; it < iters; ++it) {
+        if (live) sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
+        gs.sync();
+        const float ap = dot_split<FP, R>(ar, srow, sv);
+        const float pap = gsum128(p * ap, red, slot, gs);
+        if (!(pap > 0.f)) break;
+        const float alpha = rsold / pap;
+        xi = fmaf(alpha, p, xi);
+        r = fmaf(-alpha, ap, r);
+        const float rsnew = gsum128(r * r, red, slot, gs);
+        if (rsnew < tol) break;
+        const float beta = rsnew / rsold;
+        rsold = rsnew;
+        p = fmaf(beta, p, r);
+    }
+    return xi;
+}
+
 // Packed lower triangle of an FP x FP factor in shared memory.  Row i (block K = i / 8) keeps
 // columns 0 .. 8(K+1)-1, so every 8 x 8 block a row touches is whole; rows are laid out one
 // after the other with 4 floats of skew each, which keeps the float4 loads of 8 consecutive

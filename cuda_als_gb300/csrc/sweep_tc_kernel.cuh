@@ -20,8 +20,13 @@ constexpr int MAX_NSTAGE = 8;
 // gathered bytes in flight per SM); the LU scratch leaves room for five stages, and so does the
 // Cholesky's except at FP = 112, where four factor groups share the SM.
 __host__ __device__ constexpr int nstage_of(int solver, int fp) {
-    return solver == 0 ? 8 : (solver == 1 && fp == 112) ? 4 : 5;
+    return solver == 0 ? (fp == 112 ? 4 : 8) : (solver == 1 && fp == 112) ? 4 : 5;
 }
+// CG at FP = 112 keeps columns [0, CG_R) of a thread's row in registers and the rest in shared
+// memory, CG_SROW floats per row (15 float4: odd, conflict-free), so four groups fit an SM.
+constexpr int CG_R = 56;
+constexpr int CG_SROW = 60;
+__host__ __device__ constexpr bool cg_split_rows(int solver, int fp) { return solver == 0 && fp == 112; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
@@ -73,7 +78,7 @@ struct GroupSmem {
 template <int FP, int SOLVER>
 struct GroupLayout {
     // Cholesky: packed L then the 8 x 8 diagonal-block inverses; LU: the square Gram (+ unused)
-    static constexpr size_t ls_floats = SOLVER == 0   ? 0
+    static constexpr size_t ls_floats = SOLVER == 0   ? (cg_split_rows(SOLVER, FP) ? 128 * CG_SROW : 0)
                                         : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
                                                       : GroupSmem<FP>::ls_floats + 8 * FP;
     static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
@@ -94,7 +99,7 @@ inline int fp_of(int f) {
 inline size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
     const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
-    return solver == 0   ? vec
+    return solver == 0   ? (cg_split_rows(solver, fp) ? 128 * (size_t)CG_SROW : 0) + vec
            : solver == 1 ? tri + 8 * (size_t)fp + vec
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
 }
@@ -112,7 +117,7 @@ inline Geometry geometry(int f, int solver) {
     // the buffer, so the MMA fills the next row while they solve; their register-resident rows
     // (168 registers a thread) allow two groups per SM.  A Cholesky group keeps its buffer until
     // refinement has re-read A, and its factor lives in shared memory: one group per buffer.
-    g.nepi = solver == SOLVER_CHOL ? g.nbuf : g.nbuf / 2;
+    g.nepi = solver == SOLVER_CHOL || cg_split_rows(solver, g.fp) ? g.nbuf : g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
     g.nthreads = 64 + 128 * g.nepi + 32 * NHELP;
     const int ns = nstage_of(solver, g.fp);
@@ -331,6 +336,32 @@ __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float
         : "memory");
 }
 
+// The split CG row at FP = 112: columns 56..111 (for shared memory) and columns 0..55 with b
+// (column bcol), one round trip each.
+__device__ __forceinline__ void tmem_ld_tail56(uint32_t taddr, float (&t)[56]) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%56];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39}, [%57];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55}, [%58];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(t[0]), "=f"(t[1]), "=f"(t[2]), "=f"(t[3]), "=f"(t[4]), "=f"(t[5]), "=f"(t[6]), "=f"(t[7]), "=f"(t[8]), "=f"(t[9]), "=f"(t[10]), "=f"(t[11]), "=f"(t[12]), "=f"(t[13]), "=f"(t[14]), "=f"(t[15]), "=f"(t[16]), "=f"(t[17]), "=f"(t[18]), "=f"(t[19]), "=f"(t[20]), "=f"(t[21]), "=f"(t[22]), "=f"(t[23]), "=f"(t[24]), "=f"(t[25]), "=f"(t[26]), "=f"(t[27]), "=f"(t[28]), "=f"(t[29]), "=f"(t[30]), "=f"(t[31]), "=f"(t[32]), "=f"(t[33]), "=f"(t[34]), "=f"(t[35]), "=f"(t[36]), "=f"(t[37]), "=f"(t[38]), "=f"(t[39]), "=f"(t[40]), "=f"(t[41]), "=f"(t[42]), "=f"(t[43]), "=f"(t[44]), "=f"(t[45]), "=f"(t[46]), "=f"(t[47]), "=f"(t[48]), "=f"(t[49]), "=f"(t[50]), "=f"(t[51]), "=f"(t[52]), "=f"(t[53]), "=f"(t[54]), "=f"(t[55])
+        : "r"(taddr + 56u), "r"(taddr + 64u), "r"(taddr + 96u)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld_head56(uint32_t taddr, uint32_t bcol, float (&a)[56], float &b) {
+    asm volatile(
+        "{\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%57];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%58];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%48,%49,%50,%51,%52,%53,%54,%55}, [%59];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%56}, [%60];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(a[32]), "=f"(a[33]), "=f"(a[34]), "=f"(a[35]), "=f"(a[36]), "=f"(a[37]), "=f"(a[38]), "=f"(a[39]), "=f"(a[40]), "=f"(a[41]), "=f"(a[42]), "=f"(a[43]), "=f"(a[44]), "=f"(a[45]), "=f"(a[46]), "=f"(a[47]), "=f"(a[48]), "=f"(a[49]), "=f"(a[50]), "=f"(a[51]), "=f"(a[52]), "=f"(a[53]), "=f"(a[54]), "=f"(a[55]), "=f"(b)
+        : "r"(taddr + 0u), "r"(taddr + 32u), "r"(taddr + 48u), "r"(taddr + bcol)
+        : "memory");
+}
+
 // ------------------------------------------------------------------------------------- kernels
 
 // sum_j D[i][j] x_j re-read from TMEM in 16-column chunks (FP64 products and sums when WIDE)
@@ -466,6 +497,40 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // the CG warm start is a global load: issue it before the TMEM reads so they overlap
         const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
+        if constexpr (cg_split_rows(SOLVER, FP)) {
+            // columns CG_R.. of the row go to this thread's shared-memory row, the rest stays in
+            // registers; the accumulator is released once both halves are read
+            float *srow = Ls + i * CG_SROW;
+            {
+                float t[FP - CG_R];
+                tmem_ld_tail56(tb, t);
+#pragma unroll
+                for (int j = 0; j < FP - CG_R; ++j) {
+                    const int col = CG_R + j;
+                    float v = col < p.ng ? t[j] : 0.f;
+                    if (col == i) v = i < f ? v + reg : 1.f;  // identity on the padded rows
+                    t[j] = v;
+                }
+#pragma unroll
+                for (int j = 0; j < FP - CG_R; j += 4)
+                    *reinterpret_cast<float4 *>(srow + j) = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
+            }
+            float ar[CG_R];
+            float b;
+            tmem_ld_head56(tb, (uint32_t)p.ng, ar, b);
+#pragma unroll
+            for (int j = 0; j < CG_R; ++j) {
+                float v = j < p.ng ? ar[j] : 0.f;
+                if (j == i) v = i < f ? v + reg : 1.f;
+                ar[j] = v;
+            }
+            bi = i < f ? b : 0.f;
+            tc_fence_before();
+            gs.sync();
+            if (et == 0) mbar_arrive(release);
+            released = true;
+            xi = cg_split<FP, CG_R>(ar, srow, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
+        } else {
         // the Gram row (columns < ng) and b (column ng) in one or two TMEM round trips
         float a[FP];
         {
@@ -505,6 +570,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             xi = i < f ? vb[i] : 0.f;
             gs.sync();
         }
+        }
     }
     const float nonfinite = gsum128((i < f && !isfinite(xi)) ? 1.f : 0.f, red, slot, gs);
     if (!good || nonfinite > 0.f) {
@@ -517,7 +583,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 }
 
 template <int FP, int SOLVER>
-__global__ void __launch_bounds__(SOLVER == SOLVER_CHOL ? 576 + 32 * NHELP : 320 + 32 * NHELP, 1)
+__global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER, FP) ? 576 : 320) +
+                                      32 * NHELP, 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
     extern __shared__ uint8_t smem_raw[];
