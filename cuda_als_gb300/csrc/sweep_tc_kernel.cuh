@@ -393,7 +393,7 @@ __device__ __forceinline__ int lane_of(int i) { return i & 31; }
 // of the group had read its row out of TMEM); otherwise the caller releases it afterwards.
 template <int FP, int SOLVER>
 __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
-                          float *gsm, const GroupSync &gs, uint32_t release) {
+                          float *gsm, const GroupSync &gs, uint32_t release, float xw) {
     float *Ls = gsm;
     float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
@@ -495,8 +495,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         }
     } else {
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
-        // the CG warm start is a global load: issue it before the TMEM reads so they overlap
-        const float xw = (SOLVER == SOLVER_CG && i < f) ? xo[i] : 0.f;
+        // (xw, the CG warm start, was loaded by the caller as soon as the row was known)
         if constexpr (cg_split_rows(SOLVER, FP)) {
             // columns CG_R.. of the row go to this thread's shared-memory row, the rest stays in
             // registers; the accumulator is released once both halves are read
@@ -917,13 +916,17 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
             if (!group_wait(smem_u32(&acc_meta[buf]), use & 1)) { ok = false; break; }
             const Meta m = ameta[buf];
             if (m.row < 0) break;
+            // the CG warm start is an HBM load: issue it as soon as the row is known, before the
+            // wait for its Gram
+            const float xw = (SOLVER == SOLVER_CG && i < p.f && m.nu > 0)
+                                 ? p.X[(int64_t)m.row * p.f + i] : 0.f;
             if (!group_wait(smem_u32(&acc_full[buf]), use & 1)) { ok = false; break; }
             tc_fence_after();
             bool released = false;
             if (m.nu > 0) {
                 const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
                 released = solve_row<FP, SOLVER>(p, m, tb, i, et, g, gsm, gs,
-                                                 smem_u32(&acc_empty[buf]));
+                                                 smem_u32(&acc_empty[buf]), xw);
             } else if (i < p.f) {
                 p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
             }
