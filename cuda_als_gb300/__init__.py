@@ -25,7 +25,7 @@ from ._lib import Config, CsrView, lib
 __all__ = [
     "ALSError", "CALCULATE_VTVS_TYPE", "SOLVE_TYPE", "PRECISION", "Status", "als_model",
     "host_sparse_matrix", "default_config", "config_from_ini", "csr_to_csc", "degree_order",
-    "synth_generate", "synth_shape", "version", "load_dataset",
+    "synth_generate", "synth_shape", "version", "load_dataset", "partition_rows",
 ]
 
 
@@ -428,6 +428,15 @@ def degree_order(row_ptrs):
     perm = np.zeros(len(p) - 1, np.int32)
     _check(lib().als_degree_order(len(p) - 1, _ptr(p), _ptr(perm)))
     return perm
+
+
+def partition_rows(row_ptrs, nparts: int, row_weight: float = 0.0):
+    """Contiguous, weight-balanced row ranges for nparts ranks -> bounds (nparts + 1 int64)."""
+    p = np.ascontiguousarray(row_ptrs, np.int32)
+    bounds = np.zeros(nparts + 1, np.int64)
+    _check(lib().als_partition_rows(len(p) - 1, _ptr(p), int(nparts), float(row_weight),
+                                    _ptr(bounds)))
+    return bounds
 
 
 def synth_shape(config: int):

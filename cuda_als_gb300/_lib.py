@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         "als_csr_to_csc_device": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_csr_to_csc_device_noalloc": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_degree_order": ([i64, P, P], i32),
+        "als_partition_rows": ([i64, P, i32, f64, P], i32),
         "als_synth_shape": ([i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                              C.POINTER(i32), C.POINTER(f32)], i32),
         "als_synth_generate": ([i32, u64, f64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
@@ -112,5 +113,5 @@ EXPORTS = [
     "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan", "als_get_tuning",
     "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
     "als_csr_to_csc_device_noalloc",
-    "als_degree_order", "als_synth_shape", "als_synth_generate",
+    "als_degree_order", "als_partition_rows", "als_synth_shape", "als_synth_generate",
 ]

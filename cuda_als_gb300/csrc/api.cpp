@@ -793,6 +793,33 @@ extern "C" als_status als_csr_to_csc(const als_csr_view *csr, int32_t *col_ptrs,
     return ALS_OK;
 }
 
+extern "C" als_status als_partition_rows(int64_t rows, const int32_t *row_ptrs, int32_t nparts,
+                                         double row_weight, int64_t *bounds) {
+    if (rows < 0 || nparts < 1 || !bounds || (rows > 0 && !row_ptrs) || !(row_weight >= 0.0) ||
+        !std::isfinite(row_weight))
+        return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
+    std::string why;
+    if (rows > 0 && !check_ptrs(row_ptrs, rows, row_ptrs[rows], &why))
+        return set_global_error(ALS_ERR_INVALID_ARG, why);
+    const double total = rows > 0 ? (double)row_ptrs[rows] - row_ptrs[0] + row_weight * rows : 0.0;
+    bounds[0] = 0;
+    int64_t r = 0;
+    double before = 0.0;  // weight of rows [0, r)
+    for (int32_t k = 1; k < nparts; ++k) {
+        const double target = total * k / nparts;
+        // a row joins the earlier part while its midpoint lies before the target
+        while (r < rows) {
+            const double w = (double)(row_ptrs[r + 1] - row_ptrs[r]) + row_weight;
+            if (before + 0.5 * w >= target) break;
+            before += w;
+            ++r;
+        }
+        bounds[k] = r;
+    }
+    bounds[nparts] = rows;
+    return ALS_OK;
+}
+
 extern "C" als_status als_degree_order(int64_t rows, const int32_t *row_ptrs, int32_t *perm) {
     if (rows < 0 || (rows > 0 && (!row_ptrs || !perm)) || rows >= INT32_MAX)
         return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");

@@ -292,6 +292,16 @@ als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int32_t *col_p
  * out. */
 als_status als_degree_order(int64_t rows, const int32_t *row_ptrs, int32_t *perm);
 
+/* Contiguous row ranges for nparts ranks, balanced by weight: a row weighs its rating count plus
+ * row_weight (the solve's cost in rating-equivalents; 0 = balance ratings only).  Part k gets rows
+ * [bounds[k], bounds[k+1]), bounds[0] = 0, bounds[nparts] = rows; boundary k falls where the
+ * running weight crosses k/nparts of the total (a row goes to the earlier part when its midpoint
+ * lies before that point), so every boundary is within half a row's weight of its target.  Replaces the reference's equal-count m_batches / n_batches split
+ * (als_model.cu:1891-1896) for sharding a half-sweep over ranks.  Host work, HOST pointers:
+ * row_ptrs (rows + 1) in, bounds (nparts + 1) out. */
+als_status als_partition_rows(int64_t rows, const int32_t *row_ptrs, int32_t nparts,
+                              double row_weight, int64_t *bounds);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Synthetic ratings (seeded, deterministic across machines and thread counts)                */
 /* ------------------------------------------------------------------------------------------ */
