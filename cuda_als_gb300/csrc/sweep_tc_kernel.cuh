@@ -39,8 +39,17 @@ constexpr int MAX_NBUF = 4;
 constexpr int MD = 12;
 constexpr int MR = 16;
 // Extra warps that issue TMA gathers: one warp issues a tile::gather4 only every ~90 cycles, so the
-// stages are spread round-robin over the producer and NHELP gather warps.
-constexpr int NHELP = 2;
+// stages are spread round-robin over gather warps.  The Cholesky kernel takes three and leaves the
+// producer to its bookkeeping (at 672 threads a thread keeps 80 registers, which the factor fits
+// and the split-row CG does not); the CG / LU kernels have room for two, and their producer
+// gathers every third stage itself.
+__host__ __device__ constexpr int nhelp_of(int solver, int fp) {
+    (void)fp;
+    return solver == 1 ? 3 : 2;
+}
+__host__ __device__ constexpr int producer_gathers(int solver, int fp) {
+    return nhelp_of(solver, fp) == 2 ? 1 : 0;
+}
 constexpr int MRING_BYTES = MR * KC * 8 + MR * 16;   // column ids, ratings, Meta per slot
 enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2 };
 constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
@@ -119,7 +128,7 @@ inline Geometry geometry(int f, int solver) {
     // refinement has re-read A, and its factor lives in shared memory: one group per buffer.
     g.nepi = solver == SOLVER_CHOL || cg_split_rows(solver, g.fp) ? g.nbuf : g.nbuf / 2;
     g.tmem_cols = g.nbuf * g.acc_stride;
-    g.nthreads = 64 + 128 * g.nepi + 32 * NHELP;
+    g.nthreads = 64 + 128 * g.nepi + 32 * nhelp_of(solver, g.fp);
     const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
@@ -583,7 +592,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 
 template <int FP, int SOLVER>
 __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER, FP) ? 576 : 320) +
-                                      32 * NHELP, 1)
+                                      32 * nhelp_of(SOLVER, FP), 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
     extern __shared__ uint8_t smem_raw[];
@@ -773,7 +782,8 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
                 mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
             }
             __syncwarp();
-            if (it % (NHELP + 1) == 0) {  // this warp's share of the stages
+            if (producer_gathers(SOLVER, FP) &&
+                it % (nhelp_of(SOLVER, FP) + 1) == 0) {  // this warp's share of the stages
                 if (gq < nq && ga < natoms) {
                     const int32_t *q = scol + s * KC + 4 * gq;
                     const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE +
@@ -942,7 +952,8 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
         }
     } else {
         // ------------------------------------------------------------------ gather warps
-        // Warp h takes the stages t = h + 1, h + 1 + (NHELP + 1), ... once the producer has
+        // Warp h takes every NG-th stage from t = h + PG (NG gathering warps, PG = 1 when the
+        // producer gathers too), once the producer has
         // published them: it reads the stage's column ids, issues its tile::gather4 loads and
         // arrives on the stage's full barrier.  It runs until the producer has finished and every
         // published stage of its share is issued (also after an abort, so every full barrier the
@@ -952,7 +963,9 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
         const int gq = lane & 15, ga = lane >> 4;
         const uint64_t keep = l2_evict_last_policy();
         bool ok = true;
-        for (uint32_t t = (uint32_t)h + 1;; t += NHELP + 1) {
+        constexpr int PG = producer_gathers(SOLVER, FP);
+        constexpr int NG = nhelp_of(SOLVER, FP) + PG;
+        for (uint32_t t = (uint32_t)(h + PG);; t += NG) {
             int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out
             if (lane == 0) {
                 const unsigned long long t0 = now_ns();
