@@ -207,15 +207,23 @@ __global__ void expand_rows_kernel(int64_t rows, int64_t nnz, const int32_t *__r
     }
 }
 
+// (row, value) of each CSR position side by side, so the permutation gather below reads one
+// 8-byte pair (one sector) per rating instead of two 4-byte values from two arrays.
+__global__ void pack_rows_vals_kernel(int64_t nnz, const int32_t *__restrict__ coo_rows,
+                                      const float *__restrict__ val, int2 *__restrict__ pk) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
+         p += (int64_t)gridDim.x * blockDim.x)
+        pk[p] = make_int2(coo_rows[p], __float_as_int(val[p]));
+}
+
 __global__ void gather_csc_kernel(int64_t nnz, const int32_t *__restrict__ perm,
-                                  const int32_t *__restrict__ coo_rows,
-                                  const float *__restrict__ val, int32_t *__restrict__ ridx,
+                                  const int2 *__restrict__ pk, int32_t *__restrict__ ridx,
                                   float *__restrict__ cval) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz;
          p += (int64_t)gridDim.x * blockDim.x) {
-        int32_t e = perm[p];
-        ridx[p] = coo_rows[e];
-        cval[p] = val[e];
+        const int2 v = pk[perm[p]];
+        ridx[p] = v.x;
+        cval[p] = __int_as_float(v.y);
     }
 }
 
@@ -358,7 +366,10 @@ cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int
     e = radix_sort_pairs(idx, nullptr, skeys, perm, nnz, (int32_t)(cols > 0 ? cols - 1 : 0),
                          sort_scratch, st);
     if (e != cudaSuccess) return e;
-    gather_csc_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, coo_rows, val, ridx, cval);
+    // the sort's four n-int buffers are free again: the packed pairs take two of them
+    int2 *pk = reinterpret_cast<int2 *>(sort_scratch);
+    pack_rows_vals_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, coo_rows, val, pk);
+    gather_csc_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, pk, ridx, cval);
     col_ptrs_from_sorted_kernel<<<grid_for(nnz + 1, 256), 256, 0, st>>>(nnz, cols, skeys, cptr);
     return cudaGetLastError();
 }
