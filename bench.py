@@ -48,7 +48,8 @@ UNIT = "ms/epoch"
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=40,
+                   help="timed epochs (40 x ~25 ms: long enough for several clock samples)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
