@@ -26,6 +26,7 @@ __all__ = [
     "ALSError", "CALCULATE_VTVS_TYPE", "SOLVE_TYPE", "PRECISION", "Status", "als_model",
     "host_sparse_matrix", "default_config", "config_from_ini", "csr_to_csc", "degree_order",
     "synth_generate", "synth_shape", "version", "load_dataset", "partition_rows",
+    "EVENT_TYPE", "logger", "ini_get",
 ]
 
 
@@ -111,6 +112,94 @@ def config_from_ini(path: str):
                                      C.byref(nt), C.byref(ns), C.byref(runs), folder, 4096))
     return cfg, {"m": m.value, "n": n.value, "nnz_train": nt.value, "nnz_test": ns.value,
                  "als_runs": runs.value, "data_folder": folder.value.decode()}
+
+
+def ini_get(path: str, section: str, key: str) -> str:
+    """A string value of an INI file, "" when absent (INIReader::Get, main.cpp:36, :49)."""
+    buf = C.create_string_buffer(4096)
+    _check(lib().als_ini_get(os.fsencode(path), section.encode(), key.encode(), buf, 4096))
+    return buf.value.decode()
+
+
+class EVENT_TYPE(IntEnum):
+    """logger::EVENT_TYPE (logger.h:8-13)."""
+
+    ALS_UPDATE_U = 0
+    ALS_UPDATE_V = 1
+    ALS_ITER = 2
+    MF_MODEL_TRAINING = 3
+
+
+class logger:
+    """Mirror of the reference's logger (logger.h:7-48) over the library's event log.
+
+    ``logger(log_folder)`` is logger::init; ``log``, ``event_started``, ``event_finished`` and
+    ``save`` keep their meaning and CSV columns; ``run_iter`` / ``als_iter`` are the columns of the
+    following lines.  Attach it to a model with ``als_model.set_logger`` and ``train()`` writes the
+    reference's training lines and per-iteration events into it.
+    """
+
+    def __init__(self, log_folder: str = ""):
+        self._lg = C.c_void_p()
+        _check(lib().als_log_create(os.fsencode(str(log_folder)), C.byref(self._lg)))
+        self.log_folder = str(log_folder)
+
+    def close(self):
+        if getattr(self, "_lg", None) and self._lg.value:
+            lib().als_log_destroy(self._lg)
+            self._lg = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _iters(self):
+        r, a = C.c_int64(), C.c_int64()
+        _check(lib().als_log_get_iters(self._lg, C.byref(r), C.byref(a)))
+        return r.value, a.value
+
+    @property
+    def run_iter(self) -> int:
+        return self._iters()[0]
+
+    @run_iter.setter
+    def run_iter(self, v: int):
+        _check(lib().als_log_set_iters(self._lg, int(v), self._iters()[1]))
+
+    @property
+    def als_iter(self) -> int:
+        return self._iters()[1]
+
+    @als_iter.setter
+    def als_iter(self, v: int):
+        _check(lib().als_log_set_iters(self._lg, self._iters()[0], int(v)))
+
+    @property
+    def log_name(self) -> str:
+        return lib().als_log_name(self._lg).decode()
+
+    def log(self, text: str, write_cout: bool = False):
+        _check(lib().als_log_text(self._lg, text.encode(), int(bool(write_cout))))
+
+    def event_started(self, event_type):
+        _check(lib().als_log_event_started(self._lg, int(event_type)))
+
+    def event_finished(self, event_type, write_cout: bool = False):
+        _check(lib().als_log_event_finished(self._lg, int(event_type), int(bool(write_cout))))
+
+    def text(self) -> str:
+        """The CSV so far."""
+        n = C.c_size_t(0)
+        _check(lib().als_log_contents(self._lg, None, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        _check(lib().als_log_contents(self._lg, buf, C.byref(n)))
+        return buf.value.decode()
+
+    def save(self, log_path: str | None = None):
+        """Write to log_path, or to <log_folder>/<log_name> (logger::save)."""
+        _check(lib().als_log_save(self._lg, None if log_path is None else os.fsencode(str(log_path))))
 
 
 class _Pinned:
@@ -328,6 +417,14 @@ class als_model:
 
     def iterate(self, iters: int = 1):
         self._c(lib().als_iterate(self._h, int(iters)))
+
+    def set_logger(self, lg: "logger | None", iter_rmse: bool = False, write_cout: bool = False):
+        """Attach an event log: train() / iterate() then write the reference's training lines,
+        per-iteration ALS_UPDATE_U / ALS_UPDATE_V / ALS_ITER events and, with iter_rmse, the test
+        RMSE after every iteration but the last.  None detaches."""
+        self._logger = lg
+        self._c(lib().als_set_log(self._h, None if lg is None else lg._lg, int(bool(iter_rmse)),
+                                  int(bool(write_cout))))
 
     def half_sweep(self, side: int):
         """side 0 solves U given V (the U block of train), side 1 solves V given U."""

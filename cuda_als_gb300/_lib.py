@@ -90,6 +90,18 @@ def lib() -> C.CDLL:
         "als_csr_to_csc_device_noalloc": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_degree_order": ([i64, P, P], i32),
         "als_partition_rows": ([i64, P, i32, f64, P], i32),
+        "als_log_create": ([C.c_char_p, C.POINTER(P)], i32),
+        "als_log_destroy": ([P], i32),
+        "als_log_text": ([P, C.c_char_p, i32], i32),
+        "als_log_event_started": ([P, i32], i32),
+        "als_log_event_finished": ([P, i32, i32], i32),
+        "als_log_set_iters": ([P, i64, i64], i32),
+        "als_log_get_iters": ([P, C.POINTER(i64), C.POINTER(i64)], i32),
+        "als_log_name": ([P], C.c_char_p),
+        "als_log_contents": ([P, C.c_char_p, C.POINTER(SZ)], i32),
+        "als_log_save": ([P, C.c_char_p], i32),
+        "als_set_log": ([H, P, i32, i32], i32),
+        "als_ini_get": ([C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, SZ], i32),
         "als_synth_shape": ([i32, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
                              C.POINTER(i32), C.POINTER(f32)], i32),
         "als_synth_generate": ([i32, u64, f64, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
@@ -114,4 +126,7 @@ EXPORTS = [
     "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
     "als_csr_to_csc_device_noalloc",
     "als_degree_order", "als_partition_rows", "als_synth_shape", "als_synth_generate",
+    "als_log_create", "als_log_destroy", "als_log_text", "als_log_event_started",
+    "als_log_event_finished", "als_log_set_iters", "als_log_get_iters", "als_log_name",
+    "als_log_contents", "als_log_save", "als_set_log", "als_ini_get",
 ]

@@ -17,9 +17,11 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 OBJDIR = PKG / "_build" / platform.machine()  # x86-64 here, aarch64 on the GPU machine
 LIB = PKG / "libals_gb300.so"
+CLI = PKG / "als_gb300_main"
 
 SOURCES = [
     "api.cpp",
+    "eventlog.cpp",
     "sweep.cpp",
     "synth.cpp",
     "index_kernels.cu",
@@ -87,7 +89,25 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
         stamp.touch()
+    build_cli(verbose)
     return LIB
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The command-line driver (csrc/als_main.cpp, host C++ over the C ABI) next to the library."""
+    src = CSRC / "als_main.cpp"
+    if _stale(CLI, [src, LIB] + sorted(INCLUDE.glob("*.hpp")) + sorted(INCLUDE.glob("*.h"))):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        tmp = CLI.with_suffix(".tmp")
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", f"-I{INCLUDE}", str(src), "-o",
+               str(tmp), f"-L{PKG}", "-lals_gb300", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"building {CLI.name} failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

@@ -232,6 +232,20 @@ extern "C" als_status als_config_from_ini(const char *path, als_config *cfg, int
     return ALS_OK;
 }
 
+extern "C" als_status als_ini_get(const char *path, const char *section, const char *key,
+                                   char *buf, size_t len) {
+    if (!path || !section || !key || !buf || !len)
+        return set_global_error(ALS_ERR_INVALID_ARG, "null argument");
+    std::map<std::string, std::string> kv;
+    if (!parse_ini(path, &kv))
+        return set_global_error(ALS_ERR_IO, std::string("Can't load ") + path);
+    std::string k = std::string(section) + "." + key;
+    for (auto &ch : k) ch = (char)std::tolower((unsigned char)ch);
+    auto it = kv.find(k);
+    std::snprintf(buf, len, "%s", it == kv.end() ? "" : it->second.c_str());
+    return ALS_OK;
+}
+
 extern "C" als_status als_host_alloc(size_t bytes, void **out) {
     if (!out) return set_global_error(ALS_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
@@ -593,10 +607,55 @@ extern "C" als_status als_half_sweep(als_handle *h, int32_t side) {
     return check_sweep_flags(h);
 }
 
+static als_status rmse_impl(als_handle *h, bool test, double *out);
+
+// Epochs with an event log attached: als_iter = 1..iters, the ALS_ITER / ALS_UPDATE_U /
+// ALS_UPDATE_V events of als_model.cu:1792-1801, :2021-2034, :2259-2261 (each half-sweep is
+// waited for before its event finishes, so the event times its device work; no CUDA graph), the
+// optional "RMSE test" line of :2269-2274, and als_iter = 0 afterwards (:2277-2279).
+static als_status iterate_logged(als_handle *h, int32_t iters) {
+    als_log *lg = h->log;
+    const bool cout = h->log_cout;
+    for (int32_t it = 0; it < iters; ++it) {
+        als::log_set_als_iter(lg, it + 1);
+        als::log_event(lg, ALS_EVENT_ITER, false, false);
+        int64_t launches = 0;
+        for (int side = 0; side < 2; ++side) {
+            const int32_t ev = side == 0 ? ALS_EVENT_UPDATE_U : ALS_EVENT_UPDATE_V;
+            als::log_event(lg, ev, false, false);
+            als_status s = run_half_sweep(h, side);
+            if (s != ALS_OK) return s;
+            H_CUDA(h, cudaStreamSynchronize(h->stream));
+            launches += h->counters[0];
+            s = read_stage_ms(h, side);
+            if (s != ALS_OK) return s;
+            als::log_event(lg, ev, true, cout);
+        }
+        h->counters[0] = launches;
+        ++h->eager_epochs;
+        als::log_event(lg, ALS_EVENT_ITER, true, cout);
+        if (h->log_iter_rmse && it < iters - 1) {
+            double r = 0.0;
+            als_status s = rmse_impl(h, true, &r);
+            if (s != ALS_OK) return s;
+            char buf[64];
+            std::snprintf(buf, sizeof(buf), "%f", (double)(float)r);  // std::to_string(float)
+            als::log_text(lg, std::string("RMSE test: ") + buf, cout);
+        }
+    }
+    als::log_set_als_iter(lg, 0);
+    return ALS_OK;
+}
+
 extern "C" als_status als_iterate(als_handle *h, int32_t iters) {
     if (!h || iters < 0) return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
     cudaSetDevice(h->cfg.device);
     H_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, h->stream));
+    if (h->log) {
+        als_status s = iterate_logged(h, iters);
+        if (s != ALS_OK) return s;
+        return check_sweep_flags(h);
+    }
     als_status s = run_epochs(h, iters);
     if (s != ALS_OK) return s;
     H_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -609,8 +668,10 @@ extern "C" als_status als_iterate(als_handle *h, int32_t iters) {
 
 extern "C" als_status als_train(als_handle *h) {
     if (!h) return set_global_error(ALS_ERR_INVALID_ARG, "null handle");
+    if (h->log) als::log_text(h->log, "als model training started", h->log_cout);  // :1768-1770
     als_status s = als_init_factors(h);
     if (s != ALS_OK) return s;
+    if (h->log) als::log_text(h->log, "factors initialization done", h->log_cout);  // :1786-1788
     s = als_iterate(h, h->cfg.iters);
     if (s != ALS_OK) return s;
     // final result from device to host (als_model.cu:2283-2284)
@@ -619,6 +680,7 @@ extern "C" als_status als_train(als_handle *h) {
     H_CUDA(h, cudaMemcpyAsync(h->h_U.data(), h->d_U, sizeof(float) * h->m * h->f,
                               cudaMemcpyDeviceToHost, h->stream));
     H_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->log) als::log_text(h->log, "als model training done", h->log_cout);  // :2286-2288
     return ALS_OK;
 }
 

@@ -70,6 +70,10 @@ struct als_handle {
 
     TcState *tc = nullptr;
 
+    // event log attached by als_set_log (not owned): training lines, per-iteration test RMSE
+    als_log *log = nullptr;
+    bool log_iter_rmse = false, log_cout = false;
+
     ~als_handle();
 };
 
@@ -85,3 +89,10 @@ void reset_tuning(als_handle *h);
 als_status read_stage_ms(als_handle *h, int side);
 als_status check_sweep_flags(als_handle *h);
 bool tc_supported(int f);
+
+// eventlog.cpp
+namespace als {
+void log_text(als_log *lg, const std::string &text, bool write_cout);
+void log_event(als_log *lg, int32_t event, bool finished, bool write_cout);
+void log_set_als_iter(als_log *lg, int64_t als_iter);
+}  // namespace als

@@ -319,6 +319,70 @@ als_status als_synth_generate(int32_t config, uint64_t seed, double scale, int64
                               int32_t *col_idxs, float *vals, int32_t *test_rows,
                               int32_t *test_cols, float *test_vals);
 
+/* ------------------------------------------------------------------------------------------ */
+/* Event log: the reference's timing CSV (logger.h:7-48, logger.cpp)                           */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Timed events, same integer values and names as logger::EVENT_TYPE (logger.h:8-13). */
+enum {
+    ALS_EVENT_UPDATE_U = 0,          /* "ALS_UPDATE_U": one U half-sweep                        */
+    ALS_EVENT_UPDATE_V = 1,          /* "ALS_UPDATE_V": one V half-sweep                        */
+    ALS_EVENT_ITER = 2,              /* "ALS_ITER": one ALS iteration (U then V)                */
+    ALS_EVENT_MF_MODEL_TRAINING = 3  /* "MF_MODEL_TRAINING": model construction + train()       */
+};
+
+typedef struct als_log als_log;
+
+/* An in-memory CSV log with the columns
+ *   log_name,id,run_iter,als_iter,prev_ts,curr_ts,elapsed,event_elapsed,text
+ * (timestamps: wall-clock seconds since the epoch, 6 decimals).  log_name is the UTC creation
+ * time "%Y%m%d_%H%M%S" + "_debug=false.csv".  Writes the header and the line "init logger".
+ * log_folder may be NULL or empty (save() then writes log_name in the current directory).
+ * Replaces logger::init (logger.cpp:56-73). */
+als_status als_log_create(const char *log_folder, als_log **out);
+als_status als_log_destroy(als_log *lg);
+
+/* A text line: elapsed = time since the previous text line, event_elapsed empty; the prev_ts
+ * column holds the new timestamp (as logger::log, logger.cpp:75-87).  write_cout != 0 also prints
+ * "run iter: R als iter: A elapsed: E <text>" to stdout.  Thread-safe, as are all log calls. */
+als_status als_log_text(als_log *lg, const char *text, int32_t write_cout);
+
+/* Event start / finish (logger.cpp:89-143).  The finish line has text "event <NAME> finished",
+ * event_elapsed = now - the event's start, and does not advance prev_ts. */
+als_status als_log_event_started(als_log *lg, int32_t event);
+als_status als_log_event_finished(als_log *lg, int32_t event, int32_t write_cout);
+
+/* The run_iter / als_iter columns of the following lines (logger.h:43-44, public fields there). */
+als_status als_log_set_iters(als_log *lg, int64_t run_iter, int64_t als_iter);
+als_status als_log_get_iters(const als_log *lg, int64_t *run_iter, int64_t *als_iter);
+
+/* log_name (owned by the log). */
+const char *als_log_name(const als_log *lg);
+
+/* The CSV so far: len in = capacity of buf in bytes, out = bytes needed including the NUL.
+ * buf may be NULL to query the size; a short buffer receives nothing and ALS_ERR_INVALID_ARG. */
+als_status als_log_contents(const als_log *lg, char *buf, size_t *len);
+
+/* Write the CSV to `path`, or to <log_folder>/<log_name> when path is NULL (logger::save,
+ * logger.cpp:145-153).  ALS_ERR_IO when the file cannot be written. */
+als_status als_log_save(const als_log *lg, const char *path);
+
+/* Attach a log to a handle (NULL detaches; the handle does not own it, and the log must outlive
+ * the attachment).  While attached,
+ * als_train and als_iterate write the reference's training lines (als_model.cu:1768-1787,
+ * 1792-1801, 2021-2034, 2259-2286): "als model training started", "factors initialization done",
+ * per iteration als_iter = 1..iters with ALS_UPDATE_U, ALS_UPDATE_V and ALS_ITER events (the
+ * stream is synchronised at the end of each half-sweep, so event_elapsed covers its device work;
+ * epochs run without the CUDA graph), "RMSE test: %f" after every iteration but the last when
+ * iter_rmse != 0 (the reference's CALC_ITER_RMSE build), als_iter = 0, "als model training done".
+ * write_cout != 0 echoes every line to stdout, as the reference's write_cout = true calls. */
+als_status als_set_log(als_handle *h, als_log *lg, int32_t iter_rmse, int32_t write_cout);
+
+/* A string value of an INI file ("" when the section or key is absent, as INIReader::Get with
+ * an empty default, main.cpp:36, :49).  buf receives at most len bytes (NUL-terminated). */
+als_status als_ini_get(const char *path, const char *section, const char *key, char *buf,
+                       size_t len);
+
 #ifdef __cplusplus
 }
 #endif

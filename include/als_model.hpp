@@ -7,6 +7,7 @@
 //   als_model model(train, test, f, lambda, iters, vtvs, solve, smem_col_cnt,
 //                   m_batches, n_batches);                     // als_model.h:29-32
 //   model.train(); model.rsme_test(); model.save_libmf(path);
+//   model.set_logger(g_logger);   // the lines its train() writes into the global g_logger
 //
 // Differences a caller can see: errors throw als_gb300_error (the reference exit(1)s inside
 // CUDA_CHECK, cuda_common.h:13-91); SOLVE_TYPE has two more values (CHOLESKY, AUTO); h_UT / h_VT
@@ -21,20 +22,9 @@
 #include <string>
 #include <vector>
 
+#include "als_error.hpp"
 #include "als_gb300.h"
-
-class als_gb300_error : public std::runtime_error {
-public:
-    als_gb300_error(als_status s, const std::string &what)
-        : std::runtime_error(std::string(als_status_string(s)) + ": " + what), status(s) {}
-    als_status status;
-};
-
-namespace als_gb300_detail {
-inline void check(als_status s, const als_handle *h = nullptr) {
-    if (s != ALS_OK) throw als_gb300_error(s, als_last_error(h));
-}
-}  // namespace als_gb300_detail
+#include "als_logger.hpp"
 
 // Host ratings of one matrix in page-locked memory (cudaMallocHost, as the reference), loaded
 // from the reference's raw .bin files (cuda_sparse_matrix.cpp:6-69).  CSR and COO share the
@@ -124,20 +114,17 @@ struct als_model {
     als_model(host_sparse_matrix &host_train_ratings, host_sparse_matrix &host_test_ratings,
               int f_, float lambda_, int iters_, CALCULATE_VTVS_TYPE calculate_vtvs_type_,
               SOLVE_TYPE solve_type_, int smem_col_cnt_, int m_batches_, int n_batches_)
+        : als_model(host_train_ratings, host_test_ratings,
+                    make_config(f_, lambda_, iters_, calculate_vtvs_type_, solve_type_,
+                                smem_col_cnt_, m_batches_, n_batches_)) {}
+
+    // The same from a full configuration (e.g. als_config_from_ini, [als_gb300] options included).
+    als_model(host_sparse_matrix &host_train_ratings, host_sparse_matrix &host_test_ratings,
+              const als_config &cfg)
         : m((int)host_train_ratings.row_cnt), n((int)host_train_ratings.col_cnt),
-          m_batches(m_batches_), n_batches(n_batches_), f(f_), lambda(lambda_), iters(iters_),
-          calculate_vtvs_type(calculate_vtvs_type_), solve_type(solve_type_),
-          smem_col_cnt(smem_col_cnt_) {
-        als_config cfg;
-        als_config_default(&cfg);
-        cfg.f = f_;
-        cfg.lambda = lambda_;
-        cfg.iters = iters_;
-        cfg.calculate_vtvs_type = (int32_t)calculate_vtvs_type_;
-        cfg.solve_type = (int32_t)solve_type_;
-        cfg.smem_col_cnt = smem_col_cnt_;
-        cfg.m_batches = m_batches_;
-        cfg.n_batches = n_batches_;
+          m_batches(cfg.m_batches), n_batches(cfg.n_batches), f(cfg.f), lambda(cfg.lambda),
+          iters(cfg.iters), calculate_vtvs_type((CALCULATE_VTVS_TYPE)cfg.calculate_vtvs_type),
+          solve_type((SOLVE_TYPE)cfg.solve_type), smem_col_cnt(cfg.smem_col_cnt) {
         const host_sparse_matrix &tr = host_train_ratings, &te = host_test_ratings;
         if (!tr.has_csr) throw als_gb300_error(ALS_ERR_INVALID_ARG, "train ratings need CSR");
         als_csr_view csr{(int64_t)tr.row_cnt, (int64_t)tr.col_cnt, (int64_t)tr.val_cnt,
@@ -162,8 +149,19 @@ struct als_model {
 
     // als_model.cu:1766-2289: srand(0) init, iters x (U, V) half-sweeps, factors copied to host.
     void train() {
-        als_gb300_detail::check(als_train(h_), h_);
+        if (logger_) als_gb300_detail::check(als_set_log(h_, logger_->handle(), iter_rmse_, cout_), h_);
+        const als_status s = als_train(h_);
+        if (logger_) logger_->pull();  // train() leaves als_iter = 0, as the reference's
+        als_gb300_detail::check(s, h_);
         als_gb300_detail::check(als_get_factors(h_, h_UT, h_VT), h_);
+    }
+    // Write train()'s lines into `lg` (the reference writes them into its global g_logger):
+    // per-iteration ALS_UPDATE_U / ALS_UPDATE_V / ALS_ITER events, with iter_rmse the test RMSE
+    // after every iteration but the last (its CALC_ITER_RMSE build); write_cout echoes them.
+    void set_logger(logger &lg, bool iter_rmse = false, bool write_cout = true) {
+        logger_ = &lg;
+        iter_rmse_ = iter_rmse ? 1 : 0;
+        cout_ = write_cout ? 1 : 0;
     }
     float rsme_train() { return (float)rmse(false); }
     float rsme_test() { return (float)rmse(true); }
@@ -210,6 +208,21 @@ struct als_model {
     int smem_col_cnt;
 
 private:
+    static als_config make_config(int f_, float lambda_, int iters_, CALCULATE_VTVS_TYPE vtvs,
+                                  SOLVE_TYPE solve, int smem_col_cnt_, int m_batches_,
+                                  int n_batches_) {
+        als_config cfg;
+        als_config_default(&cfg);
+        cfg.f = f_;
+        cfg.lambda = lambda_;
+        cfg.iters = iters_;
+        cfg.calculate_vtvs_type = (int32_t)vtvs;
+        cfg.solve_type = (int32_t)solve;
+        cfg.smem_col_cnt = smem_col_cnt_;
+        cfg.m_batches = m_batches_;
+        cfg.n_batches = n_batches_;
+        return cfg;
+    }
     double rmse(bool test) {
         double out = 0.0;
         als_gb300_detail::check(test ? als_rmse_test(h_, &out) : als_rmse_train(h_, &out), h_);
@@ -217,4 +230,6 @@ private:
     }
     als_handle *h_ = nullptr;
     std::vector<float> hu_, hv_;
+    logger *logger_ = nullptr;
+    int32_t iter_rmse_ = 0, cout_ = 1;
 };
