@@ -55,8 +55,9 @@ def parse_args():
     p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--precision", choices=["bf16", "fp32"], default=None)
-    p.add_argument("--solve", choices=["lu", "cg", "cholesky", "auto"], default="auto",
-                   help="solver of the measured sweep (default: per-bucket autotuned)")
+    p.add_argument("--solve", choices=["lu", "cg", "cg16", "cholesky", "auto"], default="auto",
+                   help="solver of the measured sweep (default: per-bucket autotuned; cg16 = "
+                        "the FP16-Gram CG, its products on the tensor core)")
     p.add_argument("--iters", type=int, default=None, help="iterations for the RMSE comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -291,6 +292,7 @@ def run_ours(args):
     nnz, nnz_test = info["nnz_train"], info["nnz_test"]
     iters = args.iters if args.iters is not None else 10
     solve = {"lu": ca.SOLVE_TYPE.LU, "cg": ca.SOLVE_TYPE.CUMF_ALS_CG_FP32,
+             "cg16": ca.SOLVE_TYPE.CUMF_ALS_CG_FP16,
              "cholesky": ca.SOLVE_TYPE.CHOLESKY, "auto": ca.SOLVE_TYPE.AUTO}[args.solve]
     prec_name = args.precision or ("bf16" if f <= 128 else "fp32")
     prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16}[prec_name]

@@ -482,12 +482,15 @@ class als_model:
                 for i in range(k)]
 
     def tuning(self, side: int):
-        """The autotuner's per-bucket measurements (ALS_SOLVE_AUTO): CG and Cholesky ms on the
-        tuning sweep and the relative difference of their solutions; [] when nothing was tuned."""
+        """The autotuner's per-bucket measurements (ALS_SOLVE_AUTO): FP32-CG, Cholesky and (tensor-
+        core precisions) FP16-Gram-CG ms on the tuning sweep and each CG's relative difference to
+        the Cholesky solution; negative = not measured; [] when nothing was tuned."""
         nb = C.c_int32(64)
-        cg, ch, rel = (np.zeros(64, np.float32) for _ in range(3))
-        self._c(lib().als_get_tuning(self._h, side, _ptr(cg), _ptr(ch), _ptr(rel), C.byref(nb)))
-        return [{"ms_cg": float(cg[i]), "ms_cholesky": float(ch[i]), "rel_diff": float(rel[i])}
+        cg, ch, rel, cg16, rel16 = (np.zeros(64, np.float32) for _ in range(5))
+        self._c(lib().als_get_tuning(self._h, side, _ptr(cg), _ptr(ch), _ptr(rel), _ptr(cg16),
+                                     _ptr(rel16), C.byref(nb)))
+        return [{"ms_cg": float(cg[i]), "ms_cholesky": float(ch[i]), "rel_diff": float(rel[i]),
+                 "ms_cg16": float(cg16[i]), "rel_diff_cg16": float(rel16[i])}
                 for i in range(nb.value)]
 
     def user_halfsweep_adjoint(self, rows, cols, vals):

@@ -82,7 +82,7 @@ def lib() -> C.CDLL:
         "als_get_stage_ms": ([H, C.POINTER(f64)], i32),
         "als_get_counters": ([H, C.POINTER(i64)], i32),
         "als_get_plan": ([H, i32, P, P, P, C.POINTER(i32)], i32),
-        "als_get_tuning": ([H, i32, P, P, P, C.POINTER(i32)], i32),
+        "als_get_tuning": ([H, i32, P, P, P, P, P, C.POINTER(i32)], i32),
         "als_user_halfsweep_adjoint": ([H, C.POINTER(CooView), C.POINTER(f64), P,
                                         C.POINTER(f64)], i32),
         "als_csr_to_csc": ([C.POINTER(CsrView), P, P, P], i32),

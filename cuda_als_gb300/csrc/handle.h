@@ -17,7 +17,7 @@ struct SweepBucket {
     int32_t lo = 0, hi = 0;
     int cls = 0;  // 0: degree >= 8f, 1: f <= degree < 8f, 2: degree < f
     int solver = ALS_SOLVE_CHOLESKY;
-    float ms_cg = -1.f, ms_chol = -1.f, rel = -1.f;
+    float ms_cg = -1.f, ms_chol = -1.f, rel = -1.f, ms_cg16 = -1.f, rel16 = -1.f;
 };
 
 struct als_handle {

@@ -170,29 +170,33 @@ static cudaError_t launch_bucket(als_handle *h, int side, const SweepBucket &b, 
 }
 
 // The tuning sweep of a side (ALS_SOLVE_AUTO, the side's second half-sweep: the first leaves the
-// warm start CG needs).  Every bucket runs CG and then Cholesky from the same warm start, each
-// timed with CUDA events; the bucket keeps CG where it is faster and agrees with Cholesky within
-// AUTO_TOL, Cholesky otherwise.  The factors keep the Cholesky solution and the status words
-// count the Cholesky run only.  Synchronous (the host reads the timings): never graph-captured.
+// warm start CG needs).  Every bucket runs the FP32 CG, on the tensor-core path also the
+// FP16-Gram CG (its products on the tensor core), and then Cholesky, all from the same warm
+// start and each timed with CUDA events; the bucket keeps the fastest of Cholesky and the CGs
+// that agree with it within AUTO_TOL.  The factors keep the Cholesky solution and the status
+// words count the Cholesky run only.  Synchronous (the host reads the timings): never captured.
 static als_status tune_side(als_handle *h, int side, int *launches) {
     cudaStream_t st = h->stream;
     const int64_t rows = side == 0 ? h->m : h->n;
     float *X = side == 0 ? h->d_U : h->d_V;
     const size_t xbytes = sizeof(float) * (size_t)rows * h->f;
-    float *x_prev = nullptr, *x_cg = nullptr;
+    float *x_prev = nullptr, *x_cg = nullptr, *x_cg16 = nullptr;
     double *d_diff = nullptr;
     int32_t *flags_save = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const bool with_cg16 = h->precision != ALS_PREC_FP32;
     auto cleanup = [&]() {
         if (x_prev) cudaFree(x_prev);
         if (x_cg) cudaFree(x_cg);
+        if (x_cg16) cudaFree(x_cg16);
         if (d_diff) cudaFree(d_diff);
         if (flags_save) cudaFree(flags_save);
         for (auto e : ev)
             if (e) cudaEventDestroy(e);
     };
     if (cudaMalloc(&x_prev, xbytes) != cudaSuccess || cudaMalloc(&x_cg, xbytes) != cudaSuccess ||
-        cudaMalloc(&d_diff, 2 * sizeof(double)) != cudaSuccess ||
+        (with_cg16 && cudaMalloc(&x_cg16, xbytes) != cudaSuccess) ||
+        cudaMalloc(&d_diff, 4 * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&flags_save, 4 * sizeof(int32_t)) != cudaSuccess) {
         cleanup();
         return fail(h, ALS_ERR_OUT_OF_MEMORY, "out of memory for the autotuner's factor copies");
@@ -211,15 +215,31 @@ static als_status tune_side(als_handle *h, int side, int *launches) {
         cudaMemcpyAsync(x_cg, X, xbytes, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(X, x_prev, xbytes, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(h->d_flags, flags_save, 4 * sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+        if (with_cg16) {
+            cudaEventRecord(ev[4], st);
+            e = launch_bucket(h, side, b, ALS_SOLVE_CG_FP16, (int)k, launches);
+            cudaEventRecord(ev[5], st);
+            if (e != cudaSuccess) break;
+            cudaMemcpyAsync(x_cg16, X, xbytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(X, x_prev, xbytes, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(h->d_flags, flags_save, 4 * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                            st);
+        }
         cudaEventRecord(ev[2], st);
         e = launch_bucket(h, side, b, ALS_SOLVE_CHOLESKY, (int)k, launches);
         cudaEventRecord(ev[3], st);
         if (e != cudaSuccess) break;
         e = launch_bucket_diff(h->d_order[side], b.lo, b.hi, X, x_cg, h->f, d_diff, st);
         ++*launches;
-        double diff[2] = {0.0, 0.0};
+        if (e == cudaSuccess && with_cg16) {
+            e = launch_bucket_diff(h->d_order[side], b.lo, b.hi, X, x_cg16, h->f, d_diff + 2, st);
+            ++*launches;
+        }
+        double diff[4] = {0.0, 0.0, 0.0, 0.0};
         int32_t fl[4] = {0, 0, 0, 0};
-        if (e == cudaSuccess) e = cudaMemcpyAsync(diff, d_diff, sizeof(diff), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(diff, d_diff, sizeof(double) * (with_cg16 ? 4 : 2),
+                                cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(fl, h->d_flags, sizeof(fl), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) break;
@@ -230,8 +250,20 @@ static als_status tune_side(als_handle *h, int side, int *launches) {
         cudaEventElapsedTime(&b.ms_cg, ev[0], ev[1]);
         cudaEventElapsedTime(&b.ms_chol, ev[2], ev[3]);
         b.rel = diff[1] > 0.0 ? (float)std::sqrt(diff[0] / diff[1]) : 0.f;
-        b.solver = (b.ms_cg < b.ms_chol && b.rel <= AUTO_TOL) ? ALS_SOLVE_CG_FP32
-                                                               : ALS_SOLVE_CHOLESKY;
+        if (with_cg16) {
+            cudaEventElapsedTime(&b.ms_cg16, ev[4], ev[5]);
+            b.rel16 = diff[3] > 0.0 ? (float)std::sqrt(diff[2] / diff[3]) : 0.f;
+        }
+        b.solver = ALS_SOLVE_CHOLESKY;
+        float best = b.ms_chol;
+        if (b.rel <= AUTO_TOL && b.ms_cg < best) {
+            b.solver = ALS_SOLVE_CG_FP32;
+            best = b.ms_cg;
+        }
+        if (with_cg16 && b.rel16 <= AUTO_TOL && b.ms_cg16 >= 0.f && b.ms_cg16 < best) {
+            b.solver = ALS_SOLVE_CG_FP16;
+            best = b.ms_cg16;
+        }
         h->cls_solver[side][b.cls] = b.solver;
     }
     cleanup();
@@ -358,7 +390,8 @@ extern "C" als_status als_get_plan(const als_handle *h, int32_t side, int32_t *l
 }
 
 extern "C" als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg,
-                                     float *ms_chol, float *rel, int32_t *nb) {
+                                     float *ms_chol, float *rel, float *ms_cg16, float *rel16,
+                                     int32_t *nb) {
     if (!h || !nb || (side != 0 && side != 1))
         return set_global_error(ALS_ERR_INVALID_ARG, "bad argument");
     const std::vector<SweepBucket> &plan = h->plan[side];
@@ -366,6 +399,8 @@ extern "C" als_status als_get_tuning(const als_handle *h, int32_t side, float *m
         if (ms_cg) ms_cg[k] = plan[k].ms_cg;
         if (ms_chol) ms_chol[k] = plan[k].ms_chol;
         if (rel) rel[k] = plan[k].rel;
+        if (ms_cg16) ms_cg16[k] = plan[k].ms_cg16;
+        if (rel16) rel16[k] = plan[k].rel16;
     }
     *nb = (int32_t)plan.size();
     return ALS_OK;

@@ -11,17 +11,18 @@
 //
 // One persistent CTA per SM; rows are taken from an atomic counter in descending-degree order, so
 // a 400k-rating row occupies one SM while the others drain the rest.  Warp roles:
-//   warp 0   producer: gathers the factor rows of KC = 64 ratings per stage with 16-byte cp.async
-//            into the 128-byte-swizzled MN-major layout the MMA reads, writes the ratings as row 0
-//            of a K-major tile, and signals the stage (NSTAGE-deep ring of mbarriers).
-//   warp 1   MMA issuer: per 16 ratings one M=128 x N=Ng x K=16 MMA (Gram: A = B = the gathered
-//            panel, both MN-major) and one M=128 x N=16 MMA (RHS: B = the rating tile), into one
-//            of NBUF TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
-//   warps 2.. one or two 128-thread solver warpgroups; group g takes every NEPI-th row and owns
-//            two accumulators.  Thread i loads row i of the Gram from TMEM into registers, adds
-//            lambda n_u to its diagonal and runs the selected solver; the accumulator is released
-//            only after refinement, which re-reads A from TMEM for the residual b - A x (in FP64
-//            for rows whose Cholesky diagonal ratio exceeds cond_threshold).
+//   solver warpgroups (first, group g = warps 4g..4g+3): group g takes every NEPI-th row.  Thread
+//            i reads row i of the Gram from TMEM, adds lambda n_u to its diagonal and runs the
+//            selected solver (registers / shared memory, or the tensor core for the FP16-Gram CG);
+//            Cholesky refinement re-reads A from TMEM for the residual b - A x (in FP64 for rows
+//            whose Cholesky diagonal ratio exceeds cond_threshold).
+//   producer: walks the rows' stages (KC = 64 ratings each) and copies each stage's column ids
+//            and ratings into a metadata ring MD stages ahead with cp.async, then publishes it.
+//   MMA issuer: per 16 ratings one M=128 x N=Ng x K=16 MMA (Gram: A = B = the gathered panel,
+//            both MN-major) and one M=128 x N=16 MMA (RHS: B = the rating tile), into one of
+//            NBUF TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
+//   NGATHER gather warps: take the published stages round-robin, write the rating tile (row 0 of
+//            a K-major tile), arm the stage's barrier and issue one tile::gather4 per lane.
 // Operand layout (one stage): 2 atoms of 64 features x KC ratings; atom a, rating k, feature chunk
 // c (8 features, 16 B) sits at a*8192 + (k/8)*1024 + (k%8)*128 + ((c%8) ^ (k%8))*16, i.e. the
 // canonical SWIZZLE_128B MN-major layout with LBO = 8192 (between 64-feature atoms) and
@@ -67,15 +68,15 @@ using namespace als;
 
 static int tcg_solver(int solve_type) {
     switch (solve_type) {
-    case ALS_SOLVE_CG_FP32:
-    case ALS_SOLVE_CG_FP16: return tcg::SOLVER_CG;
+    case ALS_SOLVE_CG_FP32: return tcg::SOLVER_CG;
+    case ALS_SOLVE_CG_FP16: return tcg::SOLVER_CGTC;
     case ALS_SOLVE_LU: return tcg::SOLVER_LU;
     default: return tcg::SOLVER_CHOL;
     }
 }
 struct TcState {
     CUtensorMap tmap[2];   // [side]: TMA map of d_bf[side] (64-byte aligned member first)
-    tcg::Geometry geo[3];  // per solver (CG, Cholesky, LU)
+    tcg::Geometry geo[tcg::NSOLVER];  // per solver (CG, Cholesky, LU, tensor-core CG)
     __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
     int32_t *d_work = nullptr;                     // one row counter per bucket
     int num_sms = 0;
@@ -134,7 +135,7 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     TcState *t = new TcState();
     h->tc = t;
     size_t smem_max = 0;
-    for (int sv = 0; sv < 3; ++sv) {
+    for (int sv = 0; sv < tcg::NSOLVER; ++sv) {
         t->geo[sv] = tcg::geometry(h->f, sv);
         smem_max = std::max(smem_max, t->geo[sv].smem);
     }

@@ -18,9 +18,12 @@ constexpr int KC = 64;                       // ratings per stage
 constexpr int MAX_NSTAGE = 8;
 // Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
 // gathered bytes in flight per SM); the LU scratch leaves room for five stages, and so does the
-// Cholesky's except at FP = 112, where four factor groups share the SM.
+// Cholesky's except at FP = 112, where four factor groups share the SM.  The tensor-core CG keeps
+// only a 7 KB operand tile per group.
 __host__ __device__ constexpr int nstage_of(int solver, int fp) {
-    return solver == 0 ? (fp == 112 ? 4 : 8) : (solver == 1 && fp == 112) ? 4 : 5;
+    return solver == 3 ? 6
+           : solver == 0 ? (fp == 112 ? 4 : 8)
+                         : (solver == 1 && fp == 112) ? 4 : 5;
 }
 // CG at FP = 112 keeps columns [0, CG_R) of a thread's row in registers and the rest in shared
 // memory, CG_SROW floats per row (15 float4: odd, conflict-free), so four groups fit an SM.
@@ -38,20 +41,42 @@ constexpr int MAX_NBUF = 4;
 // stages ahead of its gathers (MR slots, MR > MD), so their HBM latency never stalls the gathers.
 constexpr int MD = 12;
 constexpr int MR = 16;
-// Extra warps that issue TMA gathers: one warp issues a tile::gather4 only every ~90 cycles, so the
-// stages are spread round-robin over gather warps.  The Cholesky kernel takes three and leaves the
-// producer to its bookkeeping (at 672 threads a thread keeps 80 registers, which the factor fits
-// and the split-row CG does not); the CG / LU kernels have room for two, and their producer
-// gathers every third stage itself.
-__host__ __device__ constexpr int nhelp_of(int solver, int fp) {
-    (void)fp;
-    return solver == 1 ? 3 : 2;
-}
-__host__ __device__ constexpr int producer_gathers(int solver, int fp) {
-    return nhelp_of(solver, fp) == 2 ? 1 : 0;
-}
+// Warp roles: the solver warpgroups come first (group g = warps 4g..4g+3, so warp w reads TMEM
+// lanes 32 (w % 4) ..), then the producer (metadata look-ahead), the MMA issuer and the gather
+// warps.  One warp issues a tile::gather4 only every ~90 cycles, so the stages go round-robin to
+// several gather warps, which also write each stage's rating tile and arm its barrier.
+constexpr int MAX_NGATHER = 6;
 constexpr int MRING_BYTES = MR * KC * 8 + MR * 16;   // column ids, ratings, Meta per slot
-enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2 };
+// SOLVER_CGTC: CG on the Gram rounded to binary16's significand (the reference's FP16-Gram CG),
+// its products A p run on the tensor core from the accumulator left in TMEM.
+enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2, SOLVER_CGTC = 3 };
+constexpr int NSOLVER = 4;
+// The tensor-core CG's operand tile for p: K = FP rows (the Gram's columns) x N = 16 columns of
+// tf32, no swizzle, core matrices of 8 columns x 4 rows (16 bytes) at (k/4) * 256 + (n/8) * 128;
+// columns 0 and 1 hold p's high and low tf32 parts, the others stay zero.
+__host__ __device__ constexpr int cgtc_tile_floats(int fp) { return (fp / 4) * 64 + 64; }
+
+// TMEM accumulators (ng + 16 columns: two fit in 256 columns unless FP = 128, whose rows have
+// ng = 128) and solver groups: CG and LU read their row out of TMEM into registers at once and
+// release the buffer, so the MMA fills the next row while they solve; their register-resident
+// rows allow two groups per SM.  A Cholesky group keeps its buffer until refinement has re-read
+// A, and its factor lives in shared memory: one group per buffer; so does the split-row CG, and
+// the tensor-core CG, whose products read A from the buffer until the solve ends.
+__host__ __device__ constexpr int nbuf_of(int fp) { return fp == 128 ? 2 : 4; }
+__host__ __device__ constexpr int nepi_of(int solver, int fp) {
+    return solver == 1 || solver == 3 || cg_split_rows(solver, fp) ? nbuf_of(fp) : nbuf_of(fp) / 2;
+}
+// Gather warps: as many as the registers the solvers need allow.  A launch's registers are
+// shared out per four warps, so above 640 threads a thread keeps 80 and at 640 it keeps 96: the
+// tensor-core CG (about 60 a thread) takes six, the other solvers two (the split-row CG and the
+// Cholesky factor need 96 and 84 at four groups).
+__host__ __device__ constexpr int ngather_of(int solver, int fp) {
+    return solver == 3 ? 6 : 2;
+}
+__host__ __device__ constexpr int nthreads_of(int solver, int fp) {
+    return 128 * nepi_of(solver, fp) + 32 * (2 + ngather_of(solver, fp));
+}
+
 constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
 
 struct Meta {  // per stage / per accumulator
@@ -89,8 +114,12 @@ struct GroupLayout {
     // Cholesky: packed L then the 8 x 8 diagonal-block inverses; LU: the square Gram (+ unused)
     static constexpr size_t ls_floats = SOLVER == 0   ? (cg_split_rows(SOLVER, FP) ? 128 * CG_SROW : 0)
                                         : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
+                                        : SOLVER == 3 ? cgtc_tile_floats(FP)
                                                       : GroupSmem<FP>::ls_floats + 8 * FP;
-    static constexpr size_t floats = ls_floats + 2 * FP + 16 + 5 * 128 + 64;
+    // (the tensor-core CG's groups start on 128-byte boundaries: its tile is an MMA operand)
+    static constexpr size_t floats =
+        SOLVER == 3 ? (ls_floats + 2 * FP + 16 + 5 * 128 + 64 + 31) / 32 * 32
+                    : ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
 struct Geometry {
@@ -105,11 +134,12 @@ inline int fp_of(int f) {
     return r <= 32 ? 32 : r <= 64 ? 64 : r <= 112 ? 112 : 128;
 }
 
-inline size_t group_floats(int fp, int solver) {
+constexpr size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
     const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
     return solver == 0   ? (cg_split_rows(solver, fp) ? 128 * (size_t)CG_SROW : 0) + vec
            : solver == 1 ? tri + 8 * (size_t)fp + vec
+           : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + vec + 31) / 32 * 32
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
 }
 
@@ -120,20 +150,16 @@ inline Geometry geometry(int f, int solver) {
     g.ng = (f + 15) / 16 * 16;
     const int acc_cols = g.ng + 16;
     g.acc_stride = acc_cols <= 128 ? 128 : 256;
-    g.nbuf = acc_cols <= 128 ? 4 : 2;
     // Accumulators rotate over the groups (group g takes rows g, g + nepi, ...; row k lands in
-    // buffer k % nbuf).  CG and LU read their row out of TMEM into registers at once and release
-    // the buffer, so the MMA fills the next row while they solve; their register-resident rows
-    // (168 registers a thread) allow two groups per SM.  A Cholesky group keeps its buffer until
-    // refinement has re-read A, and its factor lives in shared memory: one group per buffer.
-    g.nepi = solver == SOLVER_CHOL || cg_split_rows(solver, g.fp) ? g.nbuf : g.nbuf / 2;
+    // buffer k % nbuf); nbuf_of(FP) agrees with acc_cols for every f of that padded size.
+    g.nbuf = nbuf_of(g.fp);
+    g.nepi = nepi_of(solver, g.fp);
     g.tmem_cols = g.nbuf * g.acc_stride;
-    g.nthreads = 64 + 128 * g.nepi + 32 * nhelp_of(solver, g.fp);
+    g.nthreads = nthreads_of(solver, g.fp);
     const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
     bytes += MRING_BYTES;                                            // metadata ring
-    bytes += sizeof(int32_t) * ns * KC;                              // column ids per stage
     bytes += 1024;                                                   // metas, barriers, scalars
     g.smem = bytes + 1024;                                           // 1024-B alignment slack
     return g;
@@ -257,6 +283,57 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
         : "memory");
 }
+// Instruction descriptor of tcgen05.mma kind::tf32: D F32, A TF32 (from TMEM), B TF32 K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+// Shared-memory descriptor without swizzle (canonical layout of 8-row x 16-byte core matrices):
+// lbo = bytes between core matrices adjacent along K, sbo = along M/N.
+__device__ __forceinline__ uint64_t sdesc_plain(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+// D (TMEM) (+)= A (TMEM, M lanes x K columns of tf32) x B (shared memory).
+__device__ __forceinline__ void mma_tf32_tmem_a(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc,
+                                                uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// Round to the nearest value with binary16's 11-bit significand (tf32), ties to even; the
+// exponent range stays FP32's.  Infinities and NaNs pass unchanged.
+__device__ __forceinline__ float tf32_rne(float x) {
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0xFFFu + ((u >> 13) & 1u)) & 0xFFFFE000u;
+    return __uint_as_float(u);
+}
+// registers -> TMEM (16 columns of this warp's 32 lanes); the caller waits with tmem_wait_st.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]),
+        "f"(v[8]), "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float &a, float &b) {
+    asm volatile(
+        "{\n\ttcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=f"(a), "=f"(b)
+        : "r"(taddr)
+        : "memory");
+}
+
 // TMEM -> registers.  The load and its wait::ld sit in one asm block, so the outputs are only
 // defined once the data has arrived.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
@@ -397,12 +474,87 @@ __device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *
 
 __device__ __forceinline__ int lane_of(int i) { return i & 31; }
 
+// The tensor-core CG's per-group state that outlives a row: the phase of its product barrier, and
+// whether the leader's last commit has not been seen to complete (drained before the CTA ends).
+struct CgTcState {
+    uint32_t phase = 0;
+    bool unconfirmed = false;
+};
+
+// CG of cumf_als_cg/cg.cu:236-300 (the FP16-Gram variant: the regularised Gram held to binary16's
+// 11-bit significand, vectors and sums in FP32; same recurrences, warm start, step cap and
+// r'r < tol exit as the FP32 CG, cg.cu:37-232) with every product A p on the tensor core.  The
+// regularised, rounded Gram is written back into its accumulator (columns [0, ng) of the buffer,
+// read as the tf32 A operand, M = 128 lanes x K = ng); p goes to the group's operand tile as two
+// tf32 columns, p = hi + lo (22 significant bits); one M = 128 x N = 16 x K = ng chain per product
+// writes A [hi lo] to columns [ng, ng + 16) (b was read from there before), and thread i sums its
+// two values.  The group's leader (et == 0) issues the chain and commits it to `bar`; every warp
+// waits on the barrier itself.  Thread i holds x_i, r_i, p_i; padded rows (i >= f) keep zeros.
+template <int FP>
+__device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, float xi, int i,
+                       int et, float *Bt, uint32_t bar, CgTcState &st, float *red,
+                       volatile int *abort, const GroupSync &gs, bool &ok) {
+    int slot = 0;
+    const int ng = p.ng;
+    const uint32_t idesc = idesc_tf32(128, 16);
+    const uint32_t bt = smem_u32(Bt);
+    const int bo = (i >> 2) * 64 + (i & 3);  // (k = i, n = 0) in the tile; n = 1 is 4 floats on
+    auto product = [&](float v) -> float {
+        if (i < ng) {
+            const float hi = tf32_rne(v);
+            Bt[bo] = hi;
+            Bt[bo + 4] = tf32_rne(v - hi);
+        }
+        fence_async_smem();  // the tile is read by the tensor core (async proxy)
+        tc_fence_before();   // the previous product's tcgen05.ld precede the next MMA
+        gs.sync();
+        if (et == 0 && !*abort) {
+            tc_fence_after();
+            for (int kk = 0; kk < ng / 8; ++kk)
+                mma_tf32_tmem_a(tcol + (uint32_t)ng, tcol + 8u * kk,
+                                sdesc_plain(bt + 512u * kk, 256, 128), idesc, kk > 0 ? 1u : 0u);
+            mma_commit(bar);
+            st.unconfirmed = true;
+        }
+        const bool done = mbar_wait_warp(bar, st.phase & 1, abort);
+        if (done) {
+            if (et == 0) st.unconfirmed = false;
+        } else {
+            ok = false;
+            if ((threadIdx.x & 31) == 0) *abort = 1;
+        }
+        ++st.phase;
+        tc_fence_after();
+        float d0, d1;
+        tmem_ld2(trow + (uint32_t)ng, d0, d1);
+        return d0 + d1;
+    };
+    float r = bi - product(xi);
+    float pv = r;
+    float rsold = gsum128(r * r, red, slot, gs);
+    for (int it = 0; it < p.cg_iters; ++it) {
+        const float ap = product(pv);
+        const float pap = gsum128(pv * ap, red, slot, gs);
+        if (!(pap > 0.f)) break;
+        const float alpha = rsold / pap;
+        xi = fmaf(alpha, pv, xi);
+        r = fmaf(-alpha, ap, r);
+        const float rsnew = gsum128(r * r, red, slot, gs);
+        if (rsnew < p.cg_tol) break;
+        const float beta = rsnew / rsold;
+        rsold = rsnew;
+        pv = fmaf(beta, pv, r);
+    }
+    return i < p.f ? xi : 0.f;
+}
+
 // The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
 // Returns true when it released the accumulator itself (arrived on `release` once every thread
 // of the group had read its row out of TMEM); otherwise the caller releases it afterwards.
 template <int FP, int SOLVER>
 __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
-                          float *gsm, const GroupSync &gs, uint32_t release, float xw) {
+                          float *gsm, const GroupSync &gs, uint32_t release, float xw,
+                          uint32_t mvbar, CgTcState &cst, volatile int *abort, bool &ok) {
     float *Ls = gsm;
     float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
@@ -502,6 +654,31 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             }
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
         }
+    } else if constexpr (SOLVER == SOLVER_CGTC) {
+        // A_ii += lambda n_u and every entry of row i rounded to tf32, written back in place as
+        // the products' A operand; b_i read from column ng before the first product overwrites it
+#pragma unroll
+        for (int c = 0; c < FP; c += 16) {
+            if (c < p.ng) {  // warp-uniform
+                float v[16];
+                tmem_ld16(tb + c, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float a = v[j];
+                    if (c + j == i && i < f) a += reg;
+                    v[j] = tf32_rne(a);
+                }
+                tmem_st16(tb + c, v);
+            }
+        }
+        {
+            float b0, b1;
+            tmem_ld2(tb + p.ng, b0, b1);
+            bi = i < f ? b0 : 0.f;
+        }
+        tmem_wait_st();
+        xi = cg_tc<FP>(p, tb & 0xFFFFu, tb, bi, i < f ? xw : 0.f, i, et, Ls, mvbar, cst, red,
+                       abort, gs, ok);
     } else {
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // (xw, the CG warm start, was loaded by the caller as soon as the row was known)
@@ -591,30 +768,38 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 }
 
 template <int FP, int SOLVER>
-__global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER, FP) ? 576 : 320) +
-                                      32 * nhelp_of(SOLVER, FP), 1)
+__global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
+    constexpr int NEPI = nepi_of(SOLVER, FP);
+    constexpr int WP = 4 * NEPI;  // producer warp; then the MMA issuer and the gather warps
+    constexpr int WM = WP + 1;
+    constexpr int WG = WP + 2;
+    constexpr int NGATHER = ngather_of(SOLVER, FP);
+    static_assert(NGATHER <= MAX_NGATHER, "");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
     float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
-    int32_t *mcol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * p.nepi);  // [MR][KC]
+    int32_t *mcol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * NEPI);    // [MR][KC]
     float *mval = reinterpret_cast<float *>(mcol + MR * KC);                            // [MR][KC]
     Meta *mmeta = reinterpret_cast<Meta *>(mval + MR * KC);                             // [MR]
-    int32_t *scol = reinterpret_cast<int32_t *>(mmeta + MR);           // [NSTAGE][KC] per stage
-    Meta *smeta = reinterpret_cast<Meta *>(scol + NSTAGE * KC);
+    Meta *smeta = reinterpret_cast<Meta *>(mmeta + MR);                                 // [NSTAGE]
     Meta *ameta = smeta + NSTAGE;
     uint64_t *bars = (uint64_t *)(ameta + MAX_NBUF);  // 16-byte aligned: Meta is 16 bytes
     uint64_t *full = bars, *empty = bars + NSTAGE;
     uint64_t *acc_full = bars + 2 * NSTAGE;
     uint64_t *acc_empty = acc_full + MAX_NBUF, *acc_meta = acc_empty + MAX_NBUF;
     uint64_t *drain = acc_meta + MAX_NBUF;
-    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    uint64_t *mvbar = drain + 1;  // [MAX_NBUF]: the tensor-core CG's product barrier per group
+    uint32_t *tmem_slot = (uint32_t *)(mvbar + MAX_NBUF);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
     volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
-    volatile int *pub = grp_ok + MAX_NBUF;  // stages the producer has set up for the gather warps
-    volatile int *fin = pub + 1;            // the producer has set up its last stage
+    volatile int *pub = grp_ok + MAX_NBUF;  // stages whose metadata has landed (producer)
+    volatile int *fin = pub + 1;            // the producer has published its last stage
+    volatile int *done = fin + 1;               // [NGATHER]: stages gather warp h has taken its
+                                                // metadata from (slot t % MR free again)
+    volatile int *armed = done + MAX_NGATHER;   // [NSTAGE]: the last stage armed in each slot
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nbuf = p.nbuf;
@@ -622,17 +807,23 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
     // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
     for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += blockDim.x)
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
+    if constexpr (SOLVER == SOLVER_CGTC) {  // the groups' operand tiles: columns 2..15 stay zero
+        for (int i = tid; i < (int)(GroupLayout<FP, SOLVER>::floats * NEPI / 4); i += blockDim.x)
+            reinterpret_cast<float4 *>(gscratch)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
-            // the producer's arrive.expect_tx, the gathering warp's arrive once it has read the
-            // stage's column ids and issued its gathers, and the TMA bytes
-            mbar_init(smem_u32(&full[s]), 2);
+            // the gathering warp's arrive.expect_tx; the TMA bytes complete the phase
+            mbar_init(smem_u32(&full[s]), 1);
             mbar_init(smem_u32(&empty[s]), 1);
+            armed[s] = -1;
         }
+        for (int h = 0; h < NGATHER; ++h) done[h] = 0;
         for (int b = 0; b < MAX_NBUF; ++b) {
             mbar_init(smem_u32(&acc_full[b]), 1);
             mbar_init(smem_u32(&acc_empty[b]), 1);
             mbar_init(smem_u32(&acc_meta[b]), 1);
+            mbar_init(smem_u32(&mvbar[b]), 1);
         }
         mbar_init(smem_u32(drain), 1);
         *abort = 0;
@@ -641,7 +832,7 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_async_smem();
-    if (warp == 1) {
+    if (warp == WM) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(tmem_slot)),
                      "r"(p.tmem_cols)
@@ -653,19 +844,16 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
-    if (warp == 0) {
+    if (warp == WP) {
         // ------------------------------------------------------------------ producer
         // Two cursors walk the same sequence of stages (KC ratings of one row each).  The
         // look-ahead cursor issues a stage's column ids and ratings as 4-byte cp.async into the
-        // metadata ring MD stages ahead, with its Meta; the gather side then only waits for that
-        // cp.async group, writes the rating tile and issues one tile::gather4 per lane (4 ratings
-        // x 64 features).  Rows come in chunks from the atomic counter (one at a time among the
-        // first `head` slots, the heaviest rows, then CH at a time), pipelined two chunks ahead
-        // so the dependent order[] -> ptr[] loads have landed when a chunk starts.
+        // metadata ring MD stages ahead, with its Meta; the publishing cursor waits for that
+        // cp.async group and publishes the stage to the gather warps, which do the rest.  Rows
+        // come in chunks from the atomic counter (one at a time among the first `head` slots, the
+        // heaviest rows, then CH at a time), pipelined two chunks ahead so the dependent
+        // order[] -> ptr[] loads have landed when a chunk starts.
         constexpr int CH = 8;
-        const int natoms = p.fst > 64 ? 2 : 1;               // 64-feature atoms per rating
-        const int gq = lane & 15, ga = lane >> 4;            // this lane's 4-rating quad, atom
-        const uint64_t keep = l2_evict_last_policy();
         const int head = 4 * (int)gridDim.x;
         int grab_size = 1;
         auto grab = [&](int &cb, int &cc) {
@@ -694,10 +882,30 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
         int aj = 0;                                          // look-ahead cursor: row of chunk
         int abase = __shfl_sync(0xffffffffu, cbeg, 0);       // and first rating of its stage
         uint32_t gen = 0;                                    // stages issued by the look-ahead
-        // issue the metadata of stage `gen`; false once no rows are left
-        auto generate = [&]() -> bool {
+        // the metadata slot of stage g is free once the gather warp of stage g - MR has taken the
+        // column ids, ratings and Meta out of it (bounded wait; false on timeout or abort)
+        auto slot_free = [&](uint32_t g) -> bool {
+            if (g < (uint32_t)MR) return true;
+            const uint32_t old = g - MR;
+            int r = 1;
+            if (lane == 0) {
+                const volatile int *d = done + old % NGATHER;
+                const unsigned long long t0 = now_ns();
+                for (uint32_t k = 0;; ++k) {
+                    if ((uint32_t)*d > old) break;
+                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) {
+                        r = 0;
+                        break;
+                    }
+                }
+                __threadfence_block();
+            }
+            return __shfl_sync(0xffffffffu, r, 0) != 0;
+        };
+        // issue the metadata of stage `gen`: 1 issued, 0 no rows left, -1 its slot never freed
+        auto generate = [&]() -> int {
             while (aj >= ccnt) {
-                if (ccnt <= 0) return false;
+                if (ccnt <= 0) return 0;
                 ccnt = n1cnt; crow = n1row; cbeg = n1beg; cend = n1end;
                 n1cnt = n2cnt; n1row = n2row;
                 n1beg = lane < n1cnt ? p.ptr[n1row] : 0;     // n2's row ids landed a chunk ago
@@ -706,9 +914,10 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
                 grab(cb, n2cnt);
                 n2row = lane < n2cnt ? p.order[cb + lane] : 0;
                 aj = 0;
-                if (ccnt <= 0) return false;
+                if (ccnt <= 0) return 0;
                 abase = __shfl_sync(0xffffffffu, cbeg, 0);
             }
+            if (!slot_free(gen)) return -1;
             const int row = __shfl_sync(0xffffffffu, crow, aj);
             const int beg = __shfl_sync(0xffffffffu, cbeg, aj);
             const int end = __shfl_sync(0xffffffffu, cend, aj);
@@ -741,107 +950,43 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
                 abase = aj < ccnt ? __shfl_sync(0xffffffffu, cbeg, aj < ccnt ? aj : 0) : 0;
             }
             ++gen;
-            return true;
+            return 1;
         };
-        bool more = true;
-        for (int k = 0; k < MD && more; ++k) more = generate();
-        uint32_t it = 0;        // stages gathered
         bool ok = true;
-        while (it < gen) {
+        int more = 1;
+        for (int k = 0; k < MD && more == 1; ++k) more = generate();
+        if (more < 0) ok = false;
+        uint32_t it = 0;  // stages published
+        while (ok && it < gen) {
             // stage it's metadata group: at most gen - it - 1 younger groups may stay pending
             if (gen - it - 1 >= (uint32_t)(MD - 1))
                 cp_wait<MD - 1>();
             else
                 cp_wait<0>();
-            __syncwarp();
-            const int s = it % NSTAGE;
-            if (it >= NSTAGE &&
-                !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
-                ok = false;
-                break;
-            }
-            const int slot = (int)(it % MR);
-            const Meta m = mmeta[slot];
-            uint8_t *tile = ring + s * STAGE_BYTES;
-            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
-            rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
-            rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
-            // the stage's column ids move to its own array: a gather warp may read them after the
-            // look-ahead has refilled the metadata slot
-            scol[s * KC + lane] = mcol[slot * KC + lane];
-            scol[s * KC + lane + 32] = mcol[slot * KC + lane + 32];
-            // the rating tile is a generic store: visible to the tensor core (async proxy) before
-            // the stage is published
-            fence_async_smem();
-            __syncwarp();
-            // the MMA reads ratings [0, 16 nk): gather 4 nk quads (the ragged tail's column ids
-            // point at the zero row), 512 bytes per quad and atom
-            const int nq = ((m.cnt + 15) >> 4) * 4;
+            __syncwarp();  // every lane's copies (and tail fills) of the stage are in place
             if (lane == 0) {
-                smeta[s] = m;
-                mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
-            }
-            __syncwarp();
-            if (producer_gathers(SOLVER, FP) &&
-                it % (nhelp_of(SOLVER, FP) + 1) == 0) {  // this warp's share of the stages
-                if (gq < nq && ga < natoms) {
-                    const int32_t *q = scol + s * KC + 4 * gq;
-                    const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE +
-                                         (gq >> 1) * ATOM_BYTES + (gq & 1) * 512;
-                    tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3],
-                                smem_u32(&full[s]), keep);
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&full[s]));
-            }
-            if (lane == 0) {  // publish the stage (its column ids, Meta and byte count are set)
                 __threadfence_block();
                 *pub = (int)(it + 1);
             }
-            __syncwarp();   // every lane has read the slot before the look-ahead refills it
+            __syncwarp();
             ++it;
-            if (more) more = generate();
+            if (more == 1) {
+                more = generate();
+                if (more < 0) ok = false;
+            }
         }
-        if (lane == 0) {  // no further stages for the gather warps
+        // nothing of this warp may be in flight when the CTA tears down
+        cp_wait<0>();
+        __syncwarp();
+        if (lane == 0) {  // *pub is now the number of stages; the gather warps add the end marker
             __threadfence_block();
             *fin = 1;
         }
-        if (ok) {  // the end marker: one stage with row = -1
-            const int s = it % NSTAGE;
-            if (it >= NSTAGE &&
-                !mbar_wait_warp(smem_u32(&empty[s]), ((it / NSTAGE) - 1) & 1, abort)) {
-                ok = false;
-            } else {
-                if (lane == 0) {
-                    Meta m;
-                    m.row = -1;
-                    m.cnt = 0;
-                    m.flags = 3;
-                    m.nu = 0;
-                    smeta[s] = m;
-                    mbar_arrive(smem_u32(&full[s]));
-                    mbar_arrive(smem_u32(&full[s]));
-                }
-                __syncwarp();
-                ++it;
-            }
-        }
-        // nothing of this warp may be in flight when the CTA tears down: the metadata copies,
-        // and the last NSTAGE stages' gathers (their full barriers complete once the bytes have
-        // landed; bounded wait, also on abort; no slot was reused after them, so each parity is
-        // unambiguous)
-        cp_wait<0>();
-        if (lane == 0) {
-            const uint32_t from = it > (uint32_t)NSTAGE ? it - NSTAGE : 0;
-            for (uint32_t u = from; u < it; ++u)
-                mbar_wait(smem_u32(&full[u % NSTAGE]), (u / NSTAGE) & 1, nullptr);
-        }
-        __syncwarp();
         if (!ok) {
             *abort = 1;
             if (lane == 0) atomicAdd(&p.flags[2], 1);
         }
-    } else if (warp == 1) {
+    } else if (warp == WM) {
         // ------------------------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc_g = idesc_bf16(128, p.ng, true, true);
@@ -864,7 +1009,7 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
                 tc_fence_after();
                 const Meta m = smeta[s];
                 if (m.row < 0) {  // end of work: one end marker per solver warpgroup
-                    for (int g = 0; g < p.nepi && ok; ++g) {
+                    for (int g = 0; g < NEPI && ok; ++g) {
                         if (!take_buffer()) { ok = false; break; }
                         ameta[buf] = m;
                         mbar_arrive(smem_u32(&acc_meta[buf]));
@@ -903,16 +1048,17 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
             }
         }
         __syncwarp();
-    } else if (warp < 2 + 4 * p.nepi) {
+    } else if (warp < WP) {
         // ------------------------------------------------------------------ solver warpgroups
-        const int g = (warp - 2) >> 2;
-        const int et = tid - 64 - 128 * g;           // 0..127 inside the group
+        const int g = warp >> 2;
+        const int et = tid - 128 * g;                // 0..127 inside the group
         const int lanegrp = (warp & 3) * 32;         // TMEM lanes this warp may read
         const int i = lanegrp + lane;                // row of the Gram held by this thread
         const GroupSync gs{1 + g};
         float *gsm = gscratch + GroupLayout<FP, SOLVER>::floats * g;
         volatile int *okflag = grp_ok + g;
         bool ok = true;
+        CgTcState cst;
         auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
             if (et == 0) *okflag = mbar_wait(bar, parity, abort) ? 1 : 0;
             gs.sync();
@@ -920,7 +1066,7 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
             gs.sync();
             return r;
         };
-        for (uint32_t acc_it = g;; acc_it += p.nepi) {
+        for (uint32_t acc_it = g;; acc_it += NEPI) {
             const uint32_t buf = acc_it % nbuf;
             const uint32_t use = acc_it / nbuf;
             if (!group_wait(smem_u32(&acc_meta[buf]), use & 1)) { ok = false; break; }
@@ -928,7 +1074,7 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
             if (m.row < 0) break;
             // the CG warm start is an HBM load: issue it as soon as the row is known, before the
             // wait for its Gram
-            const float xw = (SOLVER == SOLVER_CG && i < p.f && m.nu > 0)
+            const float xw = ((SOLVER == SOLVER_CG || SOLVER == SOLVER_CGTC) && i < p.f && m.nu > 0)
                                  ? p.X[(int64_t)m.row * p.f + i] : 0.f;
             if (!group_wait(smem_u32(&acc_full[buf]), use & 1)) { ok = false; break; }
             tc_fence_after();
@@ -936,7 +1082,8 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
             if (m.nu > 0) {
                 const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
                 released = solve_row<FP, SOLVER>(p, m, tb, i, et, g, gsm, gs,
-                                                 smem_u32(&acc_empty[buf]), xw);
+                                                 smem_u32(&acc_empty[buf]), xw,
+                                                 smem_u32(&mvbar[g]), cst, abort, ok);
             } else if (i < p.f) {
                 p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
             }
@@ -946,72 +1093,163 @@ __global__ void __launch_bounds__((SOLVER == SOLVER_CHOL || cg_split_rows(SOLVER
                 if (et == 0) mbar_arrive(smem_u32(&acc_empty[buf]));
             }
         }
-        if (!ok) {
+        // a product chain whose completion was not seen (a wait ran out) finishes before TMEM is
+        // released: after a failed wait the leader issues nothing more, so it is the last one
+        if (SOLVER == SOLVER_CGTC && et == 0 && cst.unconfirmed)
+            mbar_wait(smem_u32(&mvbar[g]), (cst.phase - 1) & 1, nullptr);
+        if (!ok) {  // (the tensor-core CG's waits are per warp: each failing warp counts)
             *abort = 1;
-            if (et == 0) atomicAdd(&p.flags[2], 1);
+            if (SOLVER == SOLVER_CGTC ? lane == 0 : et == 0) atomicAdd(&p.flags[2], 1);
         }
     } else {
         // ------------------------------------------------------------------ gather warps
-        // Warp h takes every NG-th stage from t = h + PG (NG gathering warps, PG = 1 when the
-        // producer gathers too), once the producer has
-        // published them: it reads the stage's column ids, issues its tile::gather4 loads and
-        // arrives on the stage's full barrier.  It runs until the producer has finished and every
-        // published stage of its share is issued (also after an abort, so every full barrier the
-        // producer set up completes and the final drain ends).
-        const int h = warp - (2 + 4 * p.nepi);
+        // Warp h takes every NGATHER-th stage from t = h once the producer has published it:
+        // it waits for the stage's ring slot, writes the rating tile, reads the column ids and
+        // Meta out of the metadata slot (handing the slot back), arms the stage's full barrier
+        // with the byte count and issues one tile::gather4 per lane (4 ratings x 64 features).
+        // The warp whose turn comes after the last stage writes the end marker (row = -1).
+        const int h = warp - WG;
         const int natoms = p.fst > 64 ? 2 : 1;
-        const int gq = lane & 15, ga = lane >> 4;
+        const int gq = lane & 15, ga = lane >> 4;  // this lane's 4-rating quad, atom
         const uint64_t keep = l2_evict_last_policy();
         bool ok = true;
-        constexpr int PG = producer_gathers(SOLVER, FP);
-        constexpr int NG = nhelp_of(SOLVER, FP) + PG;
-        for (uint32_t t = (uint32_t)(h + PG);; t += NG) {
-            int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out
+        for (uint32_t t = (uint32_t)h;; t += NGATHER) {
+            int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out or aborted
+            uint32_t total = 0;
             if (lane == 0) {
                 const unsigned long long t0 = now_ns();
                 for (uint32_t k = 0;; ++k) {
                     if ((uint32_t)*pub > t) { go = 1; break; }
-                    if (*fin) { go = (uint32_t)*pub > t ? 1 : 0; break; }
-                    if ((k & 255) == 255 && now_ns() - t0 > WAIT_NS) { go = -1; break; }
+                    if (*fin) {
+                        total = (uint32_t)*pub;
+                        go = total > t ? 1 : 0;
+                        break;
+                    }
+                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) { go = -1; break; }
                 }
                 __threadfence_block();
             }
             go = __shfl_sync(0xffffffffu, go, 0);
-            if (go <= 0) {
-                ok = go == 0;
+            total = __shfl_sync(0xffffffffu, total, 0);
+            if (go < 0) {
+                ok = false;
                 break;
             }
+            if (go == 0 && t != total) break;  // another warp writes the end marker
             const int s = t % NSTAGE;
-            const int nq = ((smeta[s].cnt + 15) >> 4) * 4;
-            if (gq < nq && ga < natoms) {
-                const int32_t *q = scol + s * KC + 4 * gq;
-                const uint32_t dst = smem_u32(ring + s * STAGE_BYTES) + ga * ATOM_STRIDE +
-                                     (gq >> 1) * ATOM_BYTES + (gq & 1) * 512;
-                tma_gather4(dst, &p.tmap, 64 * ga, q[0], q[1], q[2], q[3], smem_u32(&full[s]),
-                            keep);
+            if (t >= NSTAGE) {
+                // the slot's previous stage (another warp's) is armed first: then the slot's
+                // empty barrier is at most one phase behind the one waited for below, so its
+                // parity cannot match an older phase
+                int armed_ok = 1;
+                if (lane == 0) {
+                    const unsigned long long t0 = now_ns();
+                    for (uint32_t k = 0;; ++k) {
+                        if (armed[s] >= (int)(t - NSTAGE)) break;
+                        if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) {
+                            armed_ok = 0;
+                            break;
+                        }
+                    }
+                    __threadfence_block();
+                }
+                if (!__shfl_sync(0xffffffffu, armed_ok, 0)) {
+                    ok = false;
+                    break;
+                }
+            }
+            if (t >= NSTAGE &&
+                !mbar_wait_warp(smem_u32(&empty[s]), ((t / NSTAGE) - 1) & 1, abort)) {
+                ok = false;
+                break;
+            }
+            if (go == 0) {  // t == total: the end marker, one stage with row = -1
+                if (lane == 0) {
+                    Meta m;
+                    m.row = -1;
+                    m.cnt = 0;
+                    m.flags = 3;
+                    m.nu = 0;
+                    smeta[s] = m;
+                    armed[s] = (int)t;  // (its phase completes on this arrive: no bytes)
+                    mbar_arrive(smem_u32(&full[s]));
+                }
+                __syncwarp();
+                break;
+            }
+            const int slot = (int)(t % MR);
+            const Meta m = mmeta[slot];
+            uint8_t *tile = ring + s * STAGE_BYTES;
+            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
+            rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
+            rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
+            // the MMA reads ratings [0, 16 nk): gather 4 nk quads (the ragged tail's column ids
+            // point at the zero row), 512 bytes per quad and atom
+            const int nq = ((m.cnt + 15) >> 4) * 4;
+            const bool mine = gq < nq && ga < natoms;
+            int32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+            if (mine) {
+                const int32_t *q = mcol + slot * KC + 4 * gq;
+                r0 = q[0];
+                r1 = q[1];
+                r2 = q[2];
+                r3 = q[3];
+            }
+            // the rating tile is a generic store: visible to the tensor core (async proxy)
+            // before the stage can complete
+            fence_async_smem();
+            __syncwarp();  // every lane has read the metadata slot and written its ratings
+            if (lane == 0) {
+                __threadfence_block();
+                done[h] = (int)(t + 1);  // the metadata slot may be refilled
+                smeta[s] = m;
+                armed[s] = (int)t;
+                mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&full[s]));
+            if (mine) {
+                const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE + (gq >> 1) * ATOM_BYTES +
+                                     (gq & 1) * 512;
+                tma_gather4(dst, &p.tmap, 64 * ga, r0, r1, r2, r3, smem_u32(&full[s]), keep);
+            }
+            __syncwarp();
         }
         if (!ok) {
             *abort = 1;
             if (lane == 0) atomicAdd(&p.flags[2], 1);
         }
+        // no gather may be in flight when the CTA tears down: once every gather warp is done,
+        // wait for the last stage armed in each ring slot (a slot is re-armed only after the
+        // MMA consumed its previous stage, so only the last can still be landing; bounded)
+        asm volatile("bar.sync %0, %1;" ::"r"(15), "r"(32 * NGATHER) : "memory");
+        if (h == 0 && lane == 0) {
+            for (int u = 0; u < NSTAGE; ++u) {
+                const int a = armed[u];
+                if (a >= 0) mbar_wait(smem_u32(&full[u]), (uint32_t)(a / NSTAGE) & 1, nullptr);
+            }
+        }
+        __syncwarp();
     }
 
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 1)
+    if (warp == WM)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                      "r"(p.tmem_cols)
                      : "memory");
 }
 
 // Per padded size FP (one translation unit each, compiled in parallel): set the shared-memory
-// limit of the three solver variants and launch the selected one.
+// limit of the four solver variants and launch the selected one.
 template <int FP>
 cudaError_t configure_fp(size_t smem) {
+    // the host's geometry and the kernel's per-group layout agree
+    static_assert(group_floats(FP, SOLVER_CG) == GroupLayout<FP, SOLVER_CG>::floats, "");
+    static_assert(group_floats(FP, SOLVER_CHOL) == GroupLayout<FP, SOLVER_CHOL>::floats, "");
+    static_assert(group_floats(FP, SOLVER_LU) == GroupLayout<FP, SOLVER_LU>::floats, "");
+    static_assert(group_floats(FP, SOLVER_CGTC) == GroupLayout<FP, SOLVER_CGTC>::floats, "");
+    static_assert(GroupLayout<FP, SOLVER_CGTC>::floats % 32 == 0, "");
     // every variant may use up to the device's opt-in maximum; each launch asks for its own size
     int dev = 0, maxsm = 0;
     cudaGetDevice(&dev);
@@ -1025,6 +1263,9 @@ cudaError_t configure_fp(size_t smem) {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_LU>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CGTC>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     return e;
 }
 
@@ -1033,6 +1274,7 @@ void launch_fp(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
     switch (p.solve) {
     case SOLVER_CG: sweep_tc_kernel<FP, SOLVER_CG><<<grid, g.nthreads, g.smem, st>>>(p); break;
     case SOLVER_LU: sweep_tc_kernel<FP, SOLVER_LU><<<grid, g.nthreads, g.smem, st>>>(p); break;
+    case SOLVER_CGTC: sweep_tc_kernel<FP, SOLVER_CGTC><<<grid, g.nthreads, g.smem, st>>>(p); break;
     default: sweep_tc_kernel<FP, SOLVER_CHOL><<<grid, g.nthreads, g.smem, st>>>(p); break;
     }
 }

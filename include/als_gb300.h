@@ -240,13 +240,15 @@ als_status als_get_counters(const als_handle *h, int64_t out[3]);
 als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t *kind,
                         int32_t *solver, int32_t *nb);
 
-/* The autotuner's measurements per bucket of the plan (ALS_SOLVE_AUTO, tensor-core precisions):
- * ms_cg[b] / ms_chol[b] = CUDA-event time of the bucket's launch with each solver on the tuning
- * sweep (the side's second half-sweep, both from the same warm start), rel[b] = ||x_cg - x_chol||
- * / ||x_chol|| over the bucket's rows.  Negative entries: not tuned.  nb in: capacity, out: count.
- * Buckets are the rows of degree >= 8f, f <= degree < 8f and degree < f, in that order. */
+/* The autotuner's measurements per bucket of the plan (ALS_SOLVE_AUTO): ms_cg[b] / ms_chol[b] /
+ * ms_cg16[b] = CUDA-event time of the bucket's launch with the FP32 CG, Cholesky and (tensor-core
+ * precisions only) the FP16-Gram CG on the tuning sweep (the side's second half-sweep, all from
+ * the same warm start); rel[b] / rel16[b] = ||x_cg - x_chol|| / ||x_chol|| over the bucket's
+ * rows for each CG.  The bucket keeps the fastest of Cholesky and the CGs with rel <= 2e-2.
+ * Negative entries: not measured.  Any output pointer may be NULL.  nb in: capacity, out:
+ * count.  Buckets are the rows of degree >= 8f, f <= degree < 8f and degree < f, in order. */
 als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg, float *ms_chol,
-                          float *rel, int32_t *nb);
+                          float *rel, float *ms_cg16, float *rel16, int32_t *nb);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Adjoint of the user half-sweep (no reference counterpart; required by the build's spec)     */

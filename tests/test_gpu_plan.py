@@ -56,9 +56,15 @@ def test_auto_buckets_follow_degrees_and_tuner_rule(precision):
             assert len(tuning) == len(plan)
             for b, t in zip(plan, tuning):
                 assert t["ms_cg"] > 0 and t["ms_cholesky"] > 0 and t["rel_diff"] >= 0
-                want_cg = t["ms_cg"] < t["ms_cholesky"] and t["rel_diff"] <= AUTO_TOL
-                assert b["solver"] == (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32 if want_cg
-                                       else ca.SOLVE_TYPE.CHOLESKY)
+                # the FP16-Gram CG (products on the tensor core) is a candidate on that path only
+                tc = precision != ca.PRECISION.FP32
+                assert (t["ms_cg16"] > 0 and t["rel_diff_cg16"] >= 0) if tc else t["ms_cg16"] < 0
+                cands = [(t["ms_cholesky"], ca.SOLVE_TYPE.CHOLESKY)]
+                if t["rel_diff"] <= AUTO_TOL:
+                    cands.append((t["ms_cg"], ca.SOLVE_TYPE.CUMF_ALS_CG_FP32))
+                if tc and t["rel_diff_cg16"] <= AUTO_TOL:
+                    cands.append((t["ms_cg16"], ca.SOLVE_TYPE.CUMF_ALS_CG_FP16))
+                assert b["solver"] == min(cands, key=lambda c: c[0])[1]
                 assert b["kind"] == (0 if precision == ca.PRECISION.FP32 else 1)
         assert mdl.counters()["flagged_rows"] == 0
 

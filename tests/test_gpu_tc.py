@@ -103,6 +103,62 @@ def test_tc_other_solvers(solve):
     assert rel_rows(U, Ue) < tol
 
 
+def _exact_factors(rng, rows, f):
+    """Factor values k / 8 (|k| <= 6): exact in BF16, and every Gram entry, right-hand side and
+    lambda n_u (lambda = 1/16) built from them is exact in FP32."""
+    return (rng.integers(-6, 7, (rows, f)) / 8.0).astype(np.float32)
+
+
+@pytest.mark.parametrize("f", [1, 10, 16, 31, 64, 100, 127, 128])
+def test_tc_cg_fp16_runs_its_products_on_the_tensor_core(f):
+    """Solve type 1 on the tensor-core path: CG on the regularised Gram rounded to binary16's
+    significand (the reference's FP16-Gram CG, cg.cu:236-300) with every product A p on tcgen05
+    (tf32, A from TMEM), against the oracle's FP16-Gram CG, all six steps (cg_tol = 0), both
+    sides.  Rounding A to 11 significant bits is discontinuous, so the inputs are chosen to make
+    the regularised Gram exact in FP32: GPU and oracle then round the same matrix, and what is
+    left is FP32 against FP64 vector arithmetic (the FP32-CG tolerance)."""
+    rng, m, n, ptr, idx, val = stage_boundary_problem(f, seed=11)
+    lam = 1.0 / 16
+    U0, V0 = _exact_factors(rng, m, f), _exact_factors(rng, n, f)
+    with make_model(m, n, ptr, idx, val, f, lam, solve=ca.SOLVE_TYPE.CUMF_ALS_CG_FP16,
+                    cg_tol=0.0) as mdl:
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(0)
+        U, _ = mdl.get_factors()
+        assert mdl.counters()["flagged_rows"] == 0
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(1)
+        _, V = mdl.get_factors()
+    Ue = U0.copy()
+    O.half_sweep(ptr, idx, val, V0, Ue, f, lam, solve=O.CG_FP16, cg_tol=0.0)
+    assert rel_rows(U, Ue) < 1e-3
+    assert not U[np.diff(ptr) == 0].any()
+    cptr, ridx, cval = O.csr_to_csc(m, n, ptr, idx, val)
+    Ve = V0.copy()
+    O.half_sweep(cptr, ridx, cval, U0, Ve, f, lam, solve=O.CG_FP16, cg_tol=0.0)
+    assert rel_rows(V, Ve) < 1e-3
+
+
+def test_tc_cg_fp16_on_general_factors():
+    """The same on unrounded factors (f = 100): where the FP32 and FP64 Grams straddle an 11-bit
+    rounding boundary an entry differs by 2^-11, which CG carries into the row's solution, so the
+    rows are compared in bulk (an operand-layout mistake is O(1) everywhere)."""
+    f = 100
+    rng, m, n, ptr, idx, val = stage_boundary_problem(f, seed=11)
+    U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
+    V0 = (rng.standard_normal((n, f)) * 0.3).astype(np.float32)
+    with make_model(m, n, ptr, idx, val, f, solve=ca.SOLVE_TYPE.CUMF_ALS_CG_FP16,
+                    cg_tol=0.0) as mdl:
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(0)
+        U, _ = mdl.get_factors()
+    Ue = U0.copy()
+    O.half_sweep(ptr, idx, val, bf16_round(V0), Ue, f, 0.05, solve=O.CG_FP16, cg_tol=0.0)
+    d = np.asarray(U, np.float64) - Ue
+    assert np.linalg.norm(d) / np.linalg.norm(Ue) < 2e-3
+    assert rel_rows(U, Ue) < 5e-2
+
+
 def test_tc_heavy_rows_many_stages():
     """A few rows with thousands of ratings (hundreds of pipeline stages) next to tiny rows."""
     rng = np.random.default_rng(3)
