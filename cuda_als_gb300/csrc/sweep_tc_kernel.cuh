@@ -204,11 +204,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
         }
     }
 }
-// Warp-uniform wait: lane 0 waits, the outcome is broadcast (no lane can diverge on a timeout).
+// Warp-uniform wait: lane 0 waits, the outcome is broadcast (no lane can diverge on a timeout),
+// and __syncwarp orders every lane's later memory accesses after lane 0's acquire.
 __device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort) {
     int ok = 0;
     if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort) ? 1 : 0;
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok != 0;
 }
 __device__ __forceinline__ void fence_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -599,8 +602,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     }
                 }
 #pragma unroll
-                for (int j = 0; j < 32; ++j)
-                    if (c + j == i) v[j] = i < f ? v[j] + reg : 1.f;  // identity on padded rows
+                for (int j = 0; j < 32; ++j)  // padded rows (i >= f): the identity
+                    v[j] = c + j == i ? (i < f ? v[j] + reg : 1.f) : (i < f ? v[j] : 0.f);
                 if (i < FP) {
 #pragma unroll
                     for (int j = 0; j < 32 && c + j < FP; j += 4)
@@ -664,7 +667,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                 tmem_ld16(tb + c, v);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    float a = v[j];
+                    float a = i < f ? v[j] : 0.f;  // padded rows stay zero
                     if (c + j == i && i < f) a += reg;
                     v[j] = tf32_rne(a);
                 }
@@ -692,7 +695,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 #pragma unroll
                 for (int j = 0; j < FP - CG_R; ++j) {
                     const int col = CG_R + j;
-                    float v = col < p.ng ? t[j] : 0.f;
+                    float v = col < p.ng && i < f ? t[j] : 0.f;
                     if (col == i) v = i < f ? v + reg : 1.f;  // identity on the padded rows
                     t[j] = v;
                 }
@@ -705,7 +708,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             tmem_ld_head56(tb, (uint32_t)p.ng, ar, b);
 #pragma unroll
             for (int j = 0; j < CG_R; ++j) {
-                float v = j < p.ng ? ar[j] : 0.f;
+                float v = j < p.ng && i < f ? ar[j] : 0.f;
                 if (j == i) v = i < f ? v + reg : 1.f;
                 ar[j] = v;
             }
@@ -722,7 +725,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             float b;
             tmem_ld_row(tb, (uint32_t)p.ng, a, b);
 #pragma unroll
-            for (int j = 0; j < FP; ++j) a[j] = j < p.ng ? a[j] : 0.f;
+            for (int j = 0; j < FP; ++j) a[j] = j < p.ng && i < f ? a[j] : 0.f;
             bi = i < f ? b : 0.f;
         }
 #pragma unroll
@@ -1131,6 +1134,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             }
             go = __shfl_sync(0xffffffffu, go, 0);
             total = __shfl_sync(0xffffffffu, total, 0);
+            __syncwarp();  // the lanes' reads of the stage's metadata follow lane 0's acquire
             if (go < 0) {
                 ok = false;
                 break;
@@ -1178,7 +1182,15 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 break;
             }
             const int slot = (int)(t % MR);
-            const Meta m = mmeta[slot];
+            Meta m;  // read by lane 0 (which saw the stage published), handed to the warp
+            {
+                int4 w = make_int4(0, 0, 0, 0);
+                if (lane == 0) w = *reinterpret_cast<const int4 *>(&mmeta[slot]);
+                m.row = __shfl_sync(0xffffffffu, w.x, 0);
+                m.cnt = __shfl_sync(0xffffffffu, w.y, 0);
+                m.flags = __shfl_sync(0xffffffffu, w.z, 0);
+                m.nu = __shfl_sync(0xffffffffu, w.w, 0);
+            }
             uint8_t *tile = ring + s * STAGE_BYTES;
             __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
             rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
