@@ -143,20 +143,28 @@ radix_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int shift, int64_
 // Stable scatter.  Warp w of tile t owns the contiguous key range [t*4096 + w*512, +512) and
 // walks it in 16 rounds of 32; a key's rank inside its warp is (keys of the same digit in
 // earlier rounds) + (lanes below it with the same digit in this round), found with match.any.
-// The warp offsets per digit are then an exclusive prefix over warps, and the tile offset per
-// digit comes from the scanned digit-major histogram.
+// The warp offsets per digit are an exclusive prefix over warps, the tile's digit starts an
+// exclusive scan over digits.  The keys are first placed in shared memory in digit order (the
+// tile sorted by digit), then streamed out: consecutive threads write consecutive addresses of a
+// digit's run, so the global stores coalesce instead of scattering 32 ways per instruction.  A
+// key's destination, goff[d] + (warp offset within d) + rank, is the same either way (stable).
 __global__ void __launch_bounds__(RADIX_THREADS)
 radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restrict__ vals_in,
                      int32_t *__restrict__ keys_out, int32_t *__restrict__ vals_out, int64_t n,
                      int shift, int64_t ntiles, const int32_t *__restrict__ hist_scan) {
     __shared__ int wcnt[RADIX_WARPS][RADIX_BINS];
     __shared__ int goff[RADIX_BINS];
+    __shared__ int tstart[RADIX_BINS];
+    __shared__ int wsum[RADIX_WARPS];
+    __shared__ int32_t skey[RADIX_TILE];
+    __shared__ int32_t sval[RADIX_TILE];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int w = 0; w < RADIX_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
     goff[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * ntiles + blockIdx.x];
     __syncthreads();
 
-    const int64_t base = (int64_t)blockIdx.x * RADIX_TILE + (int64_t)warp * RADIX_WARP_SPAN;
+    const int64_t tile0 = (int64_t)blockIdx.x * RADIX_TILE;
+    const int64_t base = tile0 + (int64_t)warp * RADIX_WARP_SPAN;
     const unsigned lt_mask = (1u << lane) - 1u;
     int32_t key[RADIX_ROUNDS], val[RADIX_ROUNDS];
     int rank[RADIX_ROUNDS];
@@ -176,22 +184,42 @@ radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restr
         __syncwarp();
     }
     __syncthreads();
-    {   // exclusive prefix over warps for digit threadIdx.x
-        int run = 0;
-        for (int w = 0; w < RADIX_WARPS; ++w) {
-            int t = wcnt[w][threadIdx.x];
-            wcnt[w][threadIdx.x] = run;
-            run += t;
+    int cnt = 0;  // keys of digit threadIdx.x in this tile
+    for (int w = 0; w < RADIX_WARPS; ++w) {  // exclusive prefix over warps for digit threadIdx.x
+        const int t = wcnt[w][threadIdx.x];
+        wcnt[w][threadIdx.x] = cnt;
+        cnt += t;
+    }
+    {   // tstart = exclusive scan of cnt over the 256 digits
+        int v = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
         }
+        if (lane == 31) wsum[warp] = v;
+        __syncthreads();
+        int add = 0;
+        for (int w = 0; w < warp; ++w) add += wsum[w];
+        tstart[threadIdx.x] = add + v - cnt;
     }
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < RADIX_ROUNDS; ++q) {
         if (rank[q] < 0) continue;
-        int d = (key[q] >> shift) & (RADIX_BINS - 1);
-        int64_t dst = (int64_t)goff[d] + wcnt[warp][d] + rank[q];
-        keys_out[dst] = key[q];
-        vals_out[dst] = val[q];
+        const int d = (key[q] >> shift) & (RADIX_BINS - 1);
+        const int lp = tstart[d] + wcnt[warp][d] + rank[q];
+        skey[lp] = key[q];
+        sval[lp] = val[q];
+    }
+    __syncthreads();
+    const int nvalid = (int)(n - tile0 < RADIX_TILE ? n - tile0 : RADIX_TILE);
+    for (int j = threadIdx.x; j < nvalid; j += RADIX_THREADS) {
+        const int32_t k = skey[j];
+        const int d = (k >> shift) & (RADIX_BINS - 1);
+        const int64_t dst = (int64_t)goff[d] + (j - tstart[d]);
+        keys_out[dst] = k;
+        vals_out[dst] = sval[j];
     }
 }
 
