@@ -415,10 +415,14 @@ static als_status upload_inputs(als_handle *h, const als_csr_view *csr, const al
             h->d_csc_perm = nullptr;
         }
     } else {
-        if (!h->d_csc_perm) H_CUDA(h, dalloc(&h->d_csc_perm, nnz));
+        // the CSC -> CSR permutation is built on demand (als_update_values) from this pattern
+        if (h->d_csc_perm) {
+            cudaFree(h->d_csc_perm);
+            h->d_csc_perm = nullptr;
+        }
         H_CUDA(h, csr_to_csc_device(m, n, nnz, h->d_csr_ptr, h->d_csr_idx, h->d_csr_val,
                                     h->d_csc_ptr, h->d_csc_idx, h->d_csc_val, h->d_scratch, st,
-                                    h->d_coo_row, h->d_csc_perm));
+                                    h->d_coo_row, nullptr));
     }
     H_CUDA(h, cudaEventRecord(h->ev_transpose[1], st));
     std::vector<int32_t> cptr((size_t)n + 1);

@@ -140,24 +140,35 @@ radix_hist_kernel(const int32_t *__restrict__ keys, int64_t n, int shift, int64_
     hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Payload words moved with the keys: pass 0 reads in[w] at the key's position (or, for word
+// `pos_word`, takes the position itself), later passes read the previous pass's outputs.
+struct Payload {
+    const int32_t *in[3];
+    int32_t *out[3];
+    int pos_word;  // -1: none
+};
+
 // Stable scatter.  Warp w of tile t owns the contiguous key range [t*4096 + w*512, +512) and
 // walks it in 16 rounds of 32; a key's rank inside its warp is (keys of the same digit in
 // earlier rounds) + (lanes below it with the same digit in this round), found with match.any.
 // The warp offsets per digit are an exclusive prefix over warps, the tile's digit starts an
-// exclusive scan over digits.  The keys are first placed in shared memory in digit order (the
-// tile sorted by digit), then streamed out: consecutive threads write consecutive addresses of a
-// digit's run, so the global stores coalesce instead of scattering 32 ways per instruction.  A
-// key's destination, goff[d] + (warp offset within d) + rank, is the same either way (stable).
+// exclusive scan over digits.  The keys and their W payload words are first placed in shared
+// memory in digit order (the tile sorted by digit), then streamed out: consecutive threads write
+// consecutive addresses of a digit's run, so the global stores coalesce instead of scattering 32
+// ways per instruction.  A key's destination, goff[d] + (warp offset within d) + rank, is the
+// same either way (stable).  Dynamic shared memory: (1 + W) x RADIX_TILE words.
+template <int W>
 __global__ void __launch_bounds__(RADIX_THREADS)
-radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restrict__ vals_in,
-                     int32_t *__restrict__ keys_out, int32_t *__restrict__ vals_out, int64_t n,
-                     int shift, int64_t ntiles, const int32_t *__restrict__ hist_scan) {
+radix_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
+                     Payload pl, int64_t n, int shift, int64_t ntiles,
+                     const int32_t *__restrict__ hist_scan) {
+    extern __shared__ int32_t tile_words[];  // skey[RADIX_TILE], then W payload tiles
     __shared__ int wcnt[RADIX_WARPS][RADIX_BINS];
     __shared__ int goff[RADIX_BINS];
     __shared__ int tstart[RADIX_BINS];
     __shared__ int wsum[RADIX_WARPS];
-    __shared__ int32_t skey[RADIX_TILE];
-    __shared__ int32_t sval[RADIX_TILE];
+    int32_t *skey = tile_words;
+    int32_t *spay = tile_words + RADIX_TILE;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int w = 0; w < RADIX_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
     goff[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * ntiles + blockIdx.x];
@@ -166,14 +177,16 @@ radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restr
     const int64_t tile0 = (int64_t)blockIdx.x * RADIX_TILE;
     const int64_t base = tile0 + (int64_t)warp * RADIX_WARP_SPAN;
     const unsigned lt_mask = (1u << lane) - 1u;
-    int32_t key[RADIX_ROUNDS], val[RADIX_ROUNDS];
+    int32_t key[RADIX_ROUNDS], pay[W][RADIX_ROUNDS];
     int rank[RADIX_ROUNDS];
 #pragma unroll
     for (int q = 0; q < RADIX_ROUNDS; ++q) {
         int64_t pos = base + q * 32 + lane;
         bool valid = pos < n;
         key[q] = valid ? keys_in[pos] : 0;
-        val[q] = valid ? (vals_in ? vals_in[pos] : (int32_t)pos) : 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+            pay[w][q] = !valid ? 0 : w == pl.pos_word ? (int32_t)pos : pl.in[w][pos];
         // invalid lanes get a private digit so they never match a real one
         int d = valid ? ((key[q] >> shift) & (RADIX_BINS - 1)) : (RADIX_BINS + lane);
         unsigned peers = __match_any_sync(0xffffffffu, d);
@@ -210,7 +223,8 @@ radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restr
         const int d = (key[q] >> shift) & (RADIX_BINS - 1);
         const int lp = tstart[d] + wcnt[warp][d] + rank[q];
         skey[lp] = key[q];
-        sval[lp] = val[q];
+#pragma unroll
+        for (int w = 0; w < W; ++w) spay[w * RADIX_TILE + lp] = pay[w][q];
     }
     __syncthreads();
     const int nvalid = (int)(n - tile0 < RADIX_TILE ? n - tile0 : RADIX_TILE);
@@ -219,8 +233,25 @@ radix_scatter_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restr
         const int d = (k >> shift) & (RADIX_BINS - 1);
         const int64_t dst = (int64_t)goff[d] + (j - tstart[d]);
         keys_out[dst] = k;
-        vals_out[dst] = sval[j];
+#pragma unroll
+        for (int w = 0; w < W; ++w) pl.out[w][dst] = spay[w * RADIX_TILE + j];
     }
+}
+
+// One scatter pass: the launch with its dynamic shared memory ((1 + W) 16 KB tiles; above the
+// default 48 KB per CTA for W >= 2, so the limit is raised first).
+template <int W>
+cudaError_t launch_scatter(const int32_t *keys_in, int32_t *keys_out, const Payload &pl, int64_t n,
+                           int shift, int64_t ntiles, const int32_t *hist, cudaStream_t st) {
+    const size_t dyn = sizeof(int32_t) * (size_t)(1 + W) * RADIX_TILE;
+    if (W >= 2) {
+        cudaError_t e = cudaFuncSetAttribute(radix_scatter_kernel<W>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
+    radix_scatter_kernel<W><<<(unsigned)ntiles, RADIX_THREADS, dyn, st>>>(keys_in, keys_out, pl, n,
+                                                                        shift, ntiles, hist);
+    return cudaGetLastError();
 }
 
 // Row pointers are clamped to [0, nnz]: a malformed pointer array can never write outside.
@@ -356,19 +387,28 @@ cudaError_t radix_sort_pairs(const int32_t *keys_in, const int32_t *vals_in, int
         cudaError_t e = exclusive_scan_i32(hist, hist, (int64_t)RADIX_BINS * ntiles, false,
                                            scan_scratch, st);
         if (e != cudaSuccess) return e;
-        radix_scatter_kernel<<<(unsigned)ntiles, RADIX_THREADS, 0, st>>>(
-            src_k, src_v, dst_k, dst_v, n, shift, ntiles, hist);
+        Payload pl{};
+        pl.in[0] = src_v;
+        pl.out[0] = dst_v;
+        pl.pos_word = src_v ? -1 : 0;  // no values given: the positions themselves
+        e = launch_scatter<1>(src_k, dst_k, pl, n, shift, ntiles, hist, st);
+        if (e != cudaSuccess) return e;
         src_k = dst_k;
         src_v = dst_v;
     }
     return cudaGetLastError();
 }
 
-size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz) {
+size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz, bool compact) {
     (void)rows;
     (void)cols;
     const size_t arr = align256(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
-    return 3 * arr + radix_sort_scratch_bytes(nnz);
+    if (compact) return 3 * arr + radix_sort_scratch_bytes(nnz);
+    // rows of the CSR, the sorted keys, two ping-pong sets of key + three payload words, the
+    // per-tile digit histogram and its scan
+    const int64_t ntiles = ceil_div(nnz > 0 ? nnz : 1, RADIX_TILE);
+    const size_t hist = (size_t)RADIX_BINS * (size_t)ntiles;
+    return 10 * arr + align256(sizeof(int32_t) * hist) + scan_scratch_bytes((int64_t)hist);
 }
 
 cudaError_t expand_rows(int64_t rows, int64_t nnz, const int32_t *ptr, int32_t *coo_rows,
@@ -381,23 +421,56 @@ cudaError_t expand_rows(int64_t rows, int64_t nnz, const int32_t *ptr, int32_t *
 cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int32_t *ptr,
                               const int32_t *idx, const float *val, int32_t *cptr,
                               int32_t *ridx, float *cval, void *scratch, cudaStream_t st,
-                              int32_t *coo_rows_out, int32_t *perm_out) {
+                              int32_t *coo_rows_out, int32_t *perm_out, bool compact) {
     if (nnz <= 0) return cudaMemsetAsync(cptr, 0, sizeof(int32_t) * (size_t)(cols + 1), st);
     const size_t arr = align256(sizeof(int32_t) * (size_t)nnz);
     char *s = (char *)scratch;
     int32_t *coo_rows = coo_rows_out ? coo_rows_out : (int32_t *)s;
     int32_t *skeys = (int32_t *)(s + arr);
-    int32_t *perm = perm_out ? perm_out : (int32_t *)(s + 2 * arr);
-    void *sort_scratch = s + 3 * arr;
     cudaError_t e = expand_rows(rows, nnz, ptr, coo_rows, st);
     if (e != cudaSuccess) return e;
-    e = radix_sort_pairs(idx, nullptr, skeys, perm, nnz, (int32_t)(cols > 0 ? cols - 1 : 0),
-                         sort_scratch, st);
-    if (e != cudaSuccess) return e;
-    // the sort's four n-int buffers are free again: the packed pairs take two of them
-    int2 *pk = reinterpret_cast<int2 *>(sort_scratch);
-    pack_rows_vals_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, coo_rows, val, pk);
-    gather_csc_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, pk, ridx, cval);
+    if (compact) {
+        // sort (column, CSR position), then gather the (row, value) pairs by that permutation
+        int32_t *perm = perm_out ? perm_out : (int32_t *)(s + 2 * arr);
+        void *sort_scratch = s + 3 * arr;
+        e = radix_sort_pairs(idx, nullptr, skeys, perm, nnz, (int32_t)(cols > 0 ? cols - 1 : 0),
+                             sort_scratch, st);
+        if (e != cudaSuccess) return e;
+        // the sort's four n-int buffers are free again: the packed pairs take two of them
+        int2 *pk = reinterpret_cast<int2 *>(sort_scratch);
+        pack_rows_vals_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, coo_rows, val, pk);
+        gather_csc_kernel<<<grid_for(nnz, 256), 256, 0, st>>>(nnz, perm, pk, ridx, cval);
+    } else {
+        // sort the columns with the rating's row and value (and its CSR position when the caller
+        // keeps the permutation) as payload: the last pass writes the CSC arrays themselves
+        int32_t *set[2][4];
+        for (int k = 0; k < 2; ++k)
+            for (int w = 0; w < 4; ++w) set[k][w] = (int32_t *)(s + (2 + 4 * k + w) * arr);
+        const int64_t ntiles = ceil_div(nnz, RADIX_TILE);
+        int32_t *hist = (int32_t *)(s + 10 * arr);
+        void *scan_scratch = s + 10 * arr + align256(sizeof(int32_t) * (size_t)RADIX_BINS * ntiles);
+        const int passes = radix_passes((int32_t)(cols > 0 ? cols - 1 : 0));
+        for (int pass = 0; pass < passes; ++pass) {
+            const bool last = pass == passes - 1;
+            const int32_t *src_k = pass == 0 ? idx : set[(pass - 1) & 1][0];
+            int32_t *dst_k = last ? skeys : set[pass & 1][0];
+            Payload pl{};
+            pl.pos_word = pass == 0 && perm_out ? 2 : -1;
+            for (int w = 0; w < 3; ++w) {
+                pl.in[w] = pass == 0 ? (w == 0 ? coo_rows : w == 1 ? (const int32_t *)val : nullptr)
+                                     : set[(pass - 1) & 1][1 + w];
+                pl.out[w] = last ? (w == 0 ? ridx : w == 1 ? (int32_t *)cval : perm_out)
+                                 : set[pass & 1][1 + w];
+            }
+            radix_hist_kernel<<<(unsigned)ntiles, RADIX_THREADS, 0, st>>>(src_k, nnz, pass * RADIX_BITS,
+                                                                         ntiles, hist);
+            e = exclusive_scan_i32(hist, hist, (int64_t)RADIX_BINS * ntiles, false, scan_scratch, st);
+            if (e != cudaSuccess) return e;
+            e = perm_out ? launch_scatter<3>(src_k, dst_k, pl, nnz, pass * RADIX_BITS, ntiles, hist, st)
+                         : launch_scatter<2>(src_k, dst_k, pl, nnz, pass * RADIX_BITS, ntiles, hist, st);
+            if (e != cudaSuccess) return e;
+        }
+    }
     col_ptrs_from_sorted_kernel<<<grid_for(nnz + 1, 256), 256, 0, st>>>(nnz, cols, skeys, cptr);
     return cudaGetLastError();
 }
@@ -483,7 +556,7 @@ extern "C" als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int
     if (csr->rows < 0 || csr->cols < 0 || csr->nnz < 0 || csr->nnz > INT32_MAX ||
         csr->rows >= INT32_MAX || csr->cols >= INT32_MAX)
         return set_global_error(ALS_ERR_INVALID_ARG, "shape out of range");
-    const size_t need = transpose_scratch_bytes(csr->rows, csr->cols, csr->nnz);
+    const size_t need = transpose_scratch_bytes(csr->rows, csr->cols, csr->nnz, true);
     if (need > NOALLOC_SCRATCH_BYTES)
         return set_global_error(
             ALS_ERR_INVALID_ARG,
@@ -512,7 +585,7 @@ extern "C" als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int
     }
     e = csr_to_csc_device(csr->rows, csr->cols, csr->nnz, csr->row_ptrs, csr->col_idxs,
                           csr->vals, col_ptrs, row_idxs, vals, scratch, (cudaStream_t)stream,
-                          nullptr, nullptr);
+                          nullptr, nullptr, /*compact=*/true);
     if (e != cudaSuccess)
         return set_global_error(ALS_ERR_CUDA, std::string("csr_to_csc: ") + cudaGetErrorString(e));
     return ALS_OK;

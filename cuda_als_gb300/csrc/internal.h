@@ -41,13 +41,15 @@ size_t scan_scratch_bytes(int64_t n);
 cudaError_t exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n, bool with_total,
                                void *scratch, cudaStream_t st);
 
-// CSR -> CSC on the device, stable.  Scratch: transpose_scratch_bytes.
-size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz);
+// CSR -> CSC on the device, stable.  Scratch: transpose_scratch_bytes (compact: the smaller
+// sort-then-gather variant, for the fixed-scratch entry point).
+size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz, bool compact = false);
 cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int32_t *ptr,
                               const int32_t *idx, const float *val, int32_t *cptr,
                               int32_t *ridx, float *cval, void *scratch, cudaStream_t st,
                               int32_t *coo_rows_out /* optional, nnz */,
-                              int32_t *perm_out /* optional, nnz: CSC position -> CSR position */);
+                              int32_t *perm_out /* optional, nnz: CSC position -> CSR position */,
+                              bool compact = false);
 
 // dst[p] = src[perm[p]]
 cudaError_t gather_f32(int64_t n, const int32_t *perm, const float *src, float *dst,

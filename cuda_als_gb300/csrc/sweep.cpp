@@ -61,16 +61,13 @@ void invalidate_graphs(als_handle *h) {
 als_status refresh_csc_values(als_handle *h) {
     cudaStream_t st = h->stream;
     if (!h->d_csc_perm) {
-        // CSC came from the caller: rebuild it (and the permutation) from the CSR.
+        // no permutation yet (the CSC came from the caller, or was built without it): rebuild
+        // the CSC and the permutation from the CSR, in the handle's transpose scratch
         cudaError_t e = cudaMalloc(&h->d_csc_perm, sizeof(int32_t) * (size_t)h->nnz);
         if (e != cudaSuccess) return fail(h, ALS_ERR_OUT_OF_MEMORY, "csc permutation");
-        void *scratch = nullptr;
-        S_CUDA(h, cudaMalloc(&scratch, transpose_scratch_bytes(h->m, h->n, h->nnz)));
         e = csr_to_csc_device(h->m, h->n, h->nnz, h->d_csr_ptr, h->d_csr_idx, h->d_csr_val,
-                              h->d_csc_ptr, h->d_csc_idx, h->d_csc_val, scratch, st, nullptr,
-                              h->d_csc_perm);
-        cudaStreamSynchronize(st);
-        cudaFree(scratch);
+                              h->d_csc_ptr, h->d_csc_idx, h->d_csc_val, h->d_scratch, st,
+                              nullptr, h->d_csc_perm);
         S_CUDA(h, e);
     } else {
         S_CUDA(h, gather_f32(h->nnz, h->d_csc_perm, h->d_csr_val, h->d_csc_val, st));
