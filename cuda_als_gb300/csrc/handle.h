@@ -59,7 +59,8 @@ struct als_handle {
     // als_iterate; dropped whenever a pointer, the data or the plan changes
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
-    int64_t eager_epochs = 0;  // epochs run without a graph (capture waits for the first one)
+    int64_t eager_epochs = 0;  // epochs run without a graph since the last invalidation
+                               // (capture waits for the first one)
     // kernel plan per side: buckets (rebuilt when the ratings change), half-sweeps since the
     // rebuild, and the autotuner's decision per degree class (kept across rating changes)
     std::vector<SweepBucket> plan[2];

@@ -54,6 +54,9 @@ void invalidate_graphs(als_handle *h) {
     if (h->graph) cudaGraphDestroy(h->graph);
     h->graph_exec = nullptr;
     h->graph = nullptr;
+    // the next capture waits for one eager epoch on the new state, so a reload followed by a
+    // single epoch (the e2e pattern) pays for no capture and instantiation
+    h->eager_epochs = 0;
     tc_invalidate_graphs(h);
 }
 
