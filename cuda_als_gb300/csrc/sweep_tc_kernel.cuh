@@ -779,6 +779,13 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     constexpr int WM = WP + 1;
     constexpr int WG = WP + 2;
     constexpr int NGATHER = ngather_of(SOLVER, FP);
+    // One MMA per 16 ratings for the Gram and the right-hand side together: the gather warp of a
+    // stage waits for its bytes, writes the stage's ratings into feature column ng of the panel
+    // (the gather left it zero: ng >= fst) and marks the stage ready; the MMA issuer waits for
+    // ready and issues M=128 x N=ng+16 (Gram in columns [0, ng), b in column ng; row ng of the
+    // accumulator then holds b^T, a padded row the solvers ignore).  Where the gather warps have
+    // the time: the tensor-core CG's six; FP = 128 (ng = 128) has no free column.
+    constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112;
     static_assert(NGATHER <= MAX_NGATHER, "");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -795,7 +802,8 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     uint64_t *acc_empty = acc_full + MAX_NBUF, *acc_meta = acc_empty + MAX_NBUF;
     uint64_t *drain = acc_meta + MAX_NBUF;
     uint64_t *mvbar = drain + 1;  // [MAX_NBUF]: the tensor-core CG's product barrier per group
-    uint32_t *tmem_slot = (uint32_t *)(mvbar + MAX_NBUF);
+    uint64_t *ready = mvbar + MAX_NBUF;  // [MAX_NSTAGE]: stage's ratings in the panel (FUSED)
+    uint32_t *tmem_slot = (uint32_t *)(ready + MAX_NSTAGE);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
     volatile int *grp_ok = abort + 1;  // per-group broadcast of the leader's wait outcome
     volatile int *pub = grp_ok + MAX_NBUF;  // stages whose metadata has landed (producer)
@@ -829,6 +837,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             mbar_init(smem_u32(&mvbar[b]), 1);
         }
         mbar_init(smem_u32(drain), 1);
+        for (int u = 0; u < MAX_NSTAGE; ++u) mbar_init(smem_u32(&ready[u]), 1);
         *abort = 0;
         *pub = 0;
         *fin = 0;
@@ -992,7 +1001,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     } else if (warp == WM) {
         // ------------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc_g = idesc_bf16(128, p.ng, true, true);
+            const uint32_t idesc_g = idesc_bf16(128, FUSED ? p.ng + 16 : p.ng, true, true);
             const uint32_t idesc_r = idesc_bf16(128, 16, true, false);
             const uint32_t ring_s = smem_u32(ring);
             uint32_t it = 0, acc_it = 0, buf = 0;
@@ -1007,7 +1016,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             };
             for (;;) {
                 const int s = it % NSTAGE;
-                if (!mbar_wait(smem_u32(&full[s]), (it / NSTAGE) & 1, abort)) { ok = false; break; }
+                if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort)) {
+                    ok = false;
+                    break;
+                }
                 fence_async_smem();
                 tc_fence_after();
                 const Meta m = smeta[s];
@@ -1027,10 +1039,14 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 const int nk = (m.cnt + 15) >> 4;
                 for (int kk = 0; kk < nk; ++kk) {
                     const uint64_t ad = sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
-                    const uint64_t rd = sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+
                     const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
                     mma_bf16(dg, ad, ad, idesc_g, accum);
-                    mma_bf16(db, ad, rd, idesc_r, accum);
+                    if (!FUSED) {
+                        const uint64_t rd =
+                            sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                        mma_bf16(db, ad, rd, idesc_r, accum);
+                    }
                 }
                 mma_commit(smem_u32(&empty[s]));
                 if (m.flags & 2) {
@@ -1177,6 +1193,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                     smeta[s] = m;
                     armed[s] = (int)t;  // (its phase completes on this arrive: no bytes)
                     mbar_arrive(smem_u32(&full[s]));
+                    if (FUSED) mbar_arrive(smem_u32(&ready[s]));
                 }
                 __syncwarp();
                 break;
@@ -1225,6 +1242,21 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 tma_gather4(dst, &p.tmap, 64 * ga, r0, r1, r2, r3, smem_u32(&full[s]), keep);
             }
             __syncwarp();
+            if constexpr (FUSED) {
+                // the stage's ratings into feature column ng, once its gathered rows have landed
+                if (!mbar_wait_warp(smem_u32(&full[s]), (t / NSTAGE) & 1, abort)) {
+                    ok = false;
+                    break;
+                }
+                const int ra = p.ng >> 6, rc = (p.ng & 63) >> 3;  // column ng: atom, chunk
+                for (int k = lane; k < 4 * nq; k += 32)
+                    *reinterpret_cast<__nv_bfloat16 *>(tile + ra * ATOM_STRIDE +
+                                                       (k >> 3) * ATOM_BYTES + (k & 7) * 128 +
+                                                       ((rc ^ (k & 7)) << 4)) = rt[k];
+                fence_async_smem();  // generic stores, read by the tensor core
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&ready[s]));
+            }
         }
         if (!ok) {
             *abort = 1;
