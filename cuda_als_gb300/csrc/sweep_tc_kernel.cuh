@@ -4,6 +4,7 @@
 
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,9 +53,9 @@ constexpr int MRING_BYTES = MR * KC * 8 + MR * 16;   // column ids, ratings, Met
 enum { SOLVER_CG = 0, SOLVER_CHOL = 1, SOLVER_LU = 2, SOLVER_CGTC = 3 };
 constexpr int NSOLVER = 4;
 // The tensor-core CG's operand tile for p: K = FP rows (the Gram's columns) x N = 16 columns of
-// tf32, no swizzle, core matrices of 8 columns x 4 rows (16 bytes) at (k/4) * 256 + (n/8) * 128;
-// columns 0 and 1 hold p's high and low tf32 parts, the others stay zero.
-__host__ __device__ constexpr int cgtc_tile_floats(int fp) { return (fp / 4) * 64 + 64; }
+// f16, no swizzle, core matrices of 8 columns x 8 rows (16 bytes) at (k/8) * 256 + (n/8) * 128;
+// columns 0 and 1 hold p's high and low f16 parts, the others stay zero.
+__host__ __device__ constexpr int cgtc_tile_floats(int fp) { return (fp / 8) * 64 + 64; }
 
 // TMEM accumulators (ng + 16 columns: two fit in 256 columns unless FP = 128, whose rows have
 // ng = 128) and solver groups: CG and LU read their row out of TMEM into registers at once and
@@ -286,11 +287,6 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
         : "memory");
 }
-// Instruction descriptor of tcgen05.mma kind::tf32: D F32, A TF32 (from TMEM), B TF32 K-major.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
-}
 // Shared-memory descriptor without swizzle (canonical layout of 8-row x 16-byte core matrices):
 // lbo = bytes between core matrices adjacent along K, sbo = along M/N.
 __device__ __forceinline__ uint64_t sdesc_plain(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -301,30 +297,33 @@ __device__ __forceinline__ uint64_t sdesc_plain(uint32_t saddr, uint32_t lbo, ui
     d |= (uint64_t)1 << 46;
     return d;
 }
-// D (TMEM) (+)= A (TMEM, M lanes x K columns of tf32) x B (shared memory).
-__device__ __forceinline__ void mma_tf32_tmem_a(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc,
-                                                uint32_t idesc, uint32_t accumulate) {
+// Instruction descriptor of tcgen05.mma kind::f16 with F16 A (from TMEM) and B (K-major), F32 D.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// D (TMEM) (+)= A (TMEM, M lanes x K f16 packed two to a column) x B (shared memory).
+__device__ __forceinline__ void mma_f16_tmem_a(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc,
+                                               uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
         "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-// Round to the nearest value with binary16's 11-bit significand (tf32), ties to even; the
-// exponent range stays FP32's.  Infinities and NaNs pass unchanged.
-__device__ __forceinline__ float tf32_rne(float x) {
-    uint32_t u = __float_as_uint(x);
-    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0xFFFu + ((u >> 13) & 1u)) & 0xFFFFE000u;
-    return __uint_as_float(u);
+// registers -> TMEM (8 columns of this warp's 32 lanes); the caller waits with tmem_wait_st.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t *v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]),
+                 "r"(v[7])
+                 : "memory");
 }
-// registers -> TMEM (16 columns of this warp's 32 lanes); the caller waits with tmem_wait_st.
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
-        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]),
-        "f"(v[8]), "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
-        : "memory");
+// 2^e as a float for |e| <= 126 (exact).
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((uint32_t)(127 + e) << 23); }
+// floor(log2(x)) of a positive normal float; 0 for zero.
+__device__ __forceinline__ int exp2_of(float x) {
+    return x > 0.f ? (int)((__float_as_uint(x) >> 23) & 0xffu) - 127 : 0;
 }
+
 __device__ __forceinline__ void tmem_wait_st() {
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
@@ -487,35 +486,40 @@ struct CgTcState {
 // CG of cumf_als_cg/cg.cu:236-300 (the FP16-Gram variant: the regularised Gram held to binary16's
 // 11-bit significand, vectors and sums in FP32; same recurrences, warm start, step cap and
 // r'r < tol exit as the FP32 CG, cg.cu:37-232) with every product A p on the tensor core.  The
-// regularised, rounded Gram is written back into its accumulator (columns [0, ng) of the buffer,
-// read as the tf32 A operand, M = 128 lanes x K = ng); p goes to the group's operand tile as two
-// tf32 columns, p = hi + lo (22 significant bits); one M = 128 x N = 16 x K = ng chain per product
-// writes A [hi lo] to columns [ng, ng + 16) (b was read from there before), and thread i sums its
-// two values.  The group's leader (et == 0) issues the chain and commits it to `bar`; every warp
-// waits on the barrier itself.  Thread i holds x_i, r_i, p_i; padded rows (i >= f) keep zeros.
+// regularised Gram, scaled by 2^-ka so its largest entry (on the diagonal) stays below 2^15, is
+// rounded to binary16 and written back into its accumulator packed two to a column (columns
+// [0, ng/2) of the buffer, read as the f16 A operand, M = 128 lanes x K = ng); p, scaled by a power
+// of two from the residual norm, goes to the group's operand tile as two f16 columns, p = hi + lo
+// (22 significant bits); one M = 128 x N = 16 x K = ng chain (ng / 16 MMAs) per product writes
+// A [hi lo] to columns [ng, ng + 16) (b was read from there before), and thread i sums its two
+// values and undoes both scales (powers of two: exact).  The scaling keeps binary16's 11-bit
+// rounding but not its exponent range: no entry overflows or loses bits to subnormals.  The
+// group's leader (et == 0) issues the chain and commits it to `bar`; every warp waits on the
+// barrier itself.  Thread i holds x_i, r_i, p_i; padded rows (i >= f) keep zeros.
 template <int FP>
 __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, float xi, int i,
-                       int et, float *Bt, uint32_t bar, CgTcState &st, float *red,
+                       int et, __half *Bh, int ka, uint32_t bar, CgTcState &st, float *red,
                        volatile int *abort, const GroupSync &gs, bool &ok) {
     int slot = 0;
     const int ng = p.ng;
-    const uint32_t idesc = idesc_tf32(128, 16);
-    const uint32_t bt = smem_u32(Bt);
-    const int bo = (i >> 2) * 64 + (i & 3);  // (k = i, n = 0) in the tile; n = 1 is 4 floats on
-    auto product = [&](float v) -> float {
+    const uint32_t idesc = idesc_f16(128, 16);
+    const uint32_t bt = smem_u32(Bh);
+    const int bo = (i >> 3) * 128 + (i & 7);  // (k = i, n = 0) in the tile; n = 1 is 8 halves on
+    auto product = [&](float v, int kp) -> float {  // v scaled by 2^kp before the split
         if (i < ng) {
-            const float hi = tf32_rne(v);
-            Bt[bo] = hi;
-            Bt[bo + 4] = tf32_rne(v - hi);
+            const float ps = v * pow2f(kp);
+            const __half hi = __float2half_rn(ps);
+            Bh[bo] = hi;
+            Bh[bo + 8] = __float2half_rn(ps - __half2float(hi));
         }
         fence_async_smem();  // the tile is read by the tensor core (async proxy)
         tc_fence_before();   // the previous product's tcgen05.ld precede the next MMA
         gs.sync();
         if (et == 0 && !*abort) {
             tc_fence_after();
-            for (int kk = 0; kk < ng / 8; ++kk)
-                mma_tf32_tmem_a(tcol + (uint32_t)ng, tcol + 8u * kk,
-                                sdesc_plain(bt + 512u * kk, 256, 128), idesc, kk > 0 ? 1u : 0u);
+            for (int kk = 0; kk < ng / 16; ++kk)
+                mma_f16_tmem_a(tcol + (uint32_t)ng, tcol + 8u * kk,
+                               sdesc_plain(bt + 512u * kk, 256, 128), idesc, kk > 0 ? 1u : 0u);
             mma_commit(bar);
             st.unconfirmed = true;
         }
@@ -530,13 +534,18 @@ __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, 
         tc_fence_after();
         float d0, d1;
         tmem_ld2(trow + (uint32_t)ng, d0, d1);
-        return d0 + d1;
+        return (d0 + d1) * pow2f(ka - kp);
     };
-    float r = bi - product(xi);
+    // the warm start is O(1) (factor values); later products scale p by its residual's RMS
+    auto scale_of = [&](float rs) -> int {
+        const int e = exp2_of(sqrtf(rs / (float)ng));
+        return e > 60 ? -60 : e < -60 ? 60 : -e;
+    };
+    float r = bi - product(xi, 0);
     float pv = r;
     float rsold = gsum128(r * r, red, slot, gs);
     for (int it = 0; it < p.cg_iters; ++it) {
-        const float ap = product(pv);
+        const float ap = product(pv, scale_of(rsold));
         const float pap = gsum128(pv * ap, red, slot, gs);
         if (!(pap > 0.f)) break;
         const float alpha = rsold / pap;
@@ -658,30 +667,51 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
         }
     } else if constexpr (SOLVER == SOLVER_CGTC) {
-        // A_ii += lambda n_u and every entry of row i rounded to tf32, written back in place as
-        // the products' A operand; b_i read from column ng before the first product overwrites it
+        // the largest entry of the regularised Gram (on its diagonal: PSD) sets the scale 2^-ka;
+        // a warp reads the two 16-column chunks holding its 32 lanes' diagonal entries
+        const int lg = i & ~31;
+        float dii = 0.f;
 #pragma unroll
-        for (int c = 0; c < FP; c += 16) {
-            if (c < p.ng) {  // warp-uniform
+        for (int h = 0; h < 32; h += 16) {
+            if (lg + h < p.ng) {  // warp-uniform
                 float v[16];
-                tmem_ld16(tb + c, v);
+                tmem_ld16(tb + lg + h, v);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float a = i < f ? v[j] : 0.f;  // padded rows stay zero
-                    if (c + j == i && i < f) a += reg;
-                    v[j] = tf32_rne(a);
-                }
-                tmem_st16(tb + c, v);
+                for (int j = 0; j < 16; ++j)
+                    if (lg + h + j == i) dii = v[j];
             }
         }
+        dii = i < f ? dii + reg : 0.f;
+        const float dmax = gmax128(dii, red, slot, gs);
+        const int ka = exp2_of(dmax) > 14 ? exp2_of(dmax) - 14 : 0;
+        const float sa = pow2f(-ka);
+        // b_i, then row i (+ lambda n_u on the diagonal) scaled, rounded to binary16 and packed
+        // into columns [0, ng/2) (each 16-column chunk is read before its 8 packed columns land)
         {
             float b0, b1;
             tmem_ld2(tb + p.ng, b0, b1);
             bi = i < f ? b0 : 0.f;
         }
+#pragma unroll
+        for (int c = 0; c < FP; c += 16) {
+            if (c < p.ng) {  // warp-uniform
+                float v[16];
+                tmem_ld16(tb + c, v);
+                uint32_t w[8];
+#pragma unroll
+                for (int j = 0; j < 16; j += 2) {
+                    float a0 = i < f ? v[j] : 0.f, a1 = i < f ? v[j + 1] : 0.f;  // padded: zero
+                    if (c + j == i && i < f) a0 += reg;
+                    if (c + j + 1 == i && i < f) a1 += reg;
+                    const __half2 h2 = __floats2half2_rn(a0 * sa, a1 * sa);  // .x = column c + j
+                    w[j >> 1] = *reinterpret_cast<const uint32_t *>(&h2);
+                }
+                tmem_st8(tb + c / 2, w);
+            }
+        }
         tmem_wait_st();
-        xi = cg_tc<FP>(p, tb & 0xFFFFu, tb, bi, i < f ? xw : 0.f, i, et, Ls, mvbar, cst, red,
-                       abort, gs, ok);
+        xi = cg_tc<FP>(p, tb & 0xFFFFu, tb, bi, i < f ? xw : 0.f, i, et,
+                       reinterpret_cast<__half *>(Ls), ka, mvbar, cst, red, abort, gs, ok);
     } else {
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // (xw, the CG warm start, was loaded by the caller as soon as the row was known)
