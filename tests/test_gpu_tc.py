@@ -113,7 +113,7 @@ def _exact_factors(rng, rows, f):
 def test_tc_cg_fp16_runs_its_products_on_the_tensor_core(f):
     """Solve type 1 on the tensor-core path: CG on the regularised Gram rounded to binary16's
     significand (the reference's FP16-Gram CG, cg.cu:236-300) with every product A p on tcgen05
-    (tf32, A from TMEM), against the oracle's FP16-Gram CG, all six steps (cg_tol = 0), both
+    (f16, the scaled Gram from TMEM), against the oracle's FP16-Gram CG, all six steps (cg_tol = 0), both
     sides.  Rounding A to 11 significant bits is discontinuous, so the inputs are chosen to make
     the regularised Gram exact in FP32: GPU and oracle then round the same matrix, and what is
     left is FP32 against FP64 vector arithmetic (the FP32-CG tolerance)."""
