@@ -8,6 +8,8 @@
 //
 //   cg_reg        warm-started CG of cumf_als_cg/cg.cu:37-232 (same recurrences, same exit rule
 //                 r'r < tol); the matvec reads p from shared memory as float4 broadcasts.
+//   cg_quad       the same CG with four rows shared by a lane quad (half of them in shared
+//                 memory): a quarter of the p reads, for rows too long to keep in registers.
 //   chol_fac      Cholesky A = L L^T of the Gram copied to a packed lower triangle in shared
 //                 memory, left-looking in blocks of 8 columns: the dot products are spread over
 //                 all 128 threads as (row, column-half) items, one thread factors and inverts
@@ -92,48 +94,61 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
     return xi;
 }
 
-// CG as cg_reg with each thread's row split: columns [0, R) in registers (ar), [R, FP) in shared
-// memory (srow: the thread's own FP - R floats, 16-byte aligned, rows an odd number of float4
-// apart so a quarter warp's float4 loads hit distinct banks).  Frees the registers that let more
-// solver groups share an SM.
-template <int FP, int R>
-__device__ __forceinline__ float dot_split(const float (&ar)[R], const float *srow,
-                                           const float *sv) {
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-#pragma unroll
-    for (int j = 0; j < R; j += 4) {
-        const float4 v = *reinterpret_cast<const float4 *>(sv + j);
-        s0 = fmaf(ar[j], v.x, s0);
-        s1 = fmaf(ar[j + 1], v.y, s1);
-        s2 = fmaf(ar[j + 2], v.z, s2);
-        s3 = fmaf(ar[j + 3], v.w, s3);
-    }
-#pragma unroll
-    for (int j = 0; j < FP - R; j += 4) {
-        const float4 a = *reinterpret_cast<const float4 *>(srow + j);
-        const float4 v = *reinterpret_cast<const float4 *>(sv + R + j);
-        s0 = fmaf(a.x, v.x, s0);
-        s1 = fmaf(a.y, v.y, s1);
-        s2 = fmaf(a.z, v.z, s2);
-        s3 = fmaf(a.w, v.w, s3);
-    }
-    return (s0 + s1) + (s2 + s3);
+// CG as cg_reg with the rows quad-blocked (FP = 112).  The four lanes 4a..4a+3 of a warp share
+// rows 4a..4a+3: lane 4a+c holds columns 16k+4c..16k+4c+3 (k < NK = FP/16) of all four, rows 4a
+// and 4a+1 in registers (ar[0], ar[1]), rows 4a+2 and 4a+3 in shared memory (slots 2k and 2k+1
+// of `sa`, the thread's own float4 in each).  A product reads FP/4 floats of p a thread, one
+// float4 per chunk shared by the four rows, where a whole row a thread needs all FP of them; the
+// quad's partial sums are then reduced and scattered so that lane 4a+c ends with row 4a+c.
+constexpr int CGQ_SLOT = 130;  // float4 a slot: 128 threads + 2 (staggers the slots' banks)
+
+__device__ __forceinline__ float4 shfl_xor4(float4 v, int m) {
+    return make_float4(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m),
+                       __shfl_xor_sync(0xffffffffu, v.z, m), __shfl_xor_sync(0xffffffffu, v.w, m));
 }
 
-template <int FP, int R>
-__device__ float cg_split(const float (&ar)[R], const float *srow, float bi, float xi, int i,
-                          float *sv, float *red, int iters, float tol, const GroupSync &gs) {
+template <int NK>
+__device__ __forceinline__ float dot_quad(const float4 (&ar)[2][NK], const float4 *sa,
+                                          const float *sv, int t) {
+    const int c = t & 3;
+    const float4 *pv = reinterpret_cast<const float4 *>(sv) + c;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int k = 0; k < NK; ++k) {
+        const float4 v = pv[4 * k];
+        const float4 s2 = sa[(2 * k) * CGQ_SLOT + t];
+        const float4 s3 = sa[(2 * k + 1) * CGQ_SLOT + t];
+        a0 = fmaf(ar[0][k].x, v.x, fmaf(ar[0][k].y, v.y, fmaf(ar[0][k].z, v.z, fmaf(ar[0][k].w, v.w, a0))));
+        a1 = fmaf(ar[1][k].x, v.x, fmaf(ar[1][k].y, v.y, fmaf(ar[1][k].z, v.z, fmaf(ar[1][k].w, v.w, a1))));
+        a2 = fmaf(s2.x, v.x, fmaf(s2.y, v.y, fmaf(s2.z, v.z, fmaf(s2.w, v.w, a2))));
+        a3 = fmaf(s3.x, v.x, fmaf(s3.y, v.y, fmaf(s3.z, v.z, fmaf(s3.w, v.w, a3))));
+    }
+    // reduce-scatter over the quad: lanes c, c^2 combine rows {0,1} (c < 2) or {2,3}, then
+    // lanes c, c^1 combine row c
+    const bool hi = (c & 2) != 0;
+    float k0 = hi ? a2 : a0, k1 = hi ? a3 : a1;
+    const float s0 = hi ? a0 : a2, s1 = hi ? a1 : a3;
+    k0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    k1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    const bool odd = (c & 1) != 0;
+    return (odd ? k1 : k0) + __shfl_xor_sync(0xffffffffu, odd ? k0 : k1, 1);
+}
+
+template <int NK>
+__device__ float cg_quad(const float4 (&ar)[2][NK], const float4 *sa, float bi, float xi, int i,
+                         float *sv, float *red, int iters, float tol, const GroupSync &gs) {
+    constexpr int FP = 16 * NK;
     int slot = 0;
     const bool live = i < FP;
     if (live) sv[i] = xi;
     gs.sync();
-    float r = bi - dot_split<FP, R>(ar, srow, sv);
+    float r = bi - dot_quad<NK>(ar, sa, sv, i);
     float p = r;
     float rsold = gsum128(r * r, red, slot, gs);
     for (int it = 0; it < iters; ++it) {
         if (live) sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
         gs.sync();
-        const float ap = dot_split<FP, R>(ar, srow, sv);
+        const float ap = dot_quad<NK>(ar, sa, sv, i);
         const float pap = gsum128(p * ap, red, slot, gs);
         if (!(pap > 0.f)) break;
         const float alpha = rsold / pap;

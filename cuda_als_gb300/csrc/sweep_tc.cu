@@ -20,7 +20,9 @@
 //            and ratings into a metadata ring MD stages ahead with cp.async, then publishes it.
 //   MMA issuer: per 16 ratings one M=128 x N=Ng x K=16 MMA (Gram: A = B = the gathered panel,
 //            both MN-major) and one M=128 x N=16 MMA (RHS: B = the rating tile), into one of
-//            NBUF TMEM accumulators; tcgen05.commit frees the stage / publishes the row.
+//            NBUF TMEM accumulators; tcgen05.commit frees the stage / publishes the row.  (The
+//            tensor-core CG at f <= 112 fuses the two: one N=Ng+16 MMA, the ratings written into
+//            feature column Ng of the panel by the gather warp once its rows have landed.)
 //   NGATHER gather warps: take the published stages round-robin, write the rating tile (row 0 of
 //            a K-major tile), arm the stage's barrier and issue one tile::gather4 per lane.
 // Operand layout (one stage): 2 atoms of 64 features x KC ratings; atom a, rating k, feature chunk

@@ -26,11 +26,10 @@ __host__ __device__ constexpr int nstage_of(int solver, int fp) {
            : solver == 0 ? (fp == 112 ? 4 : 8)
                          : (solver == 1 && fp == 112) ? 4 : 5;
 }
-// CG at FP = 112 keeps columns [0, CG_R) of a thread's row in registers and the rest in shared
-// memory, CG_SROW floats per row (15 float4: odd, conflict-free), so four groups fit an SM.
-constexpr int CG_R = 56;
-constexpr int CG_SROW = 60;
+// CG at FP = 112 quad-blocks its rows (cg_quad): half of a row's values in registers, half in
+// shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups fit an SM.
 __host__ __device__ constexpr bool cg_split_rows(int solver, int fp) { return solver == 0 && fp == 112; }
+__host__ __device__ constexpr int cgq_floats(int fp) { return 2 * (fp / 16) * 130 * 4; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
@@ -113,7 +112,7 @@ struct GroupSmem {
 template <int FP, int SOLVER>
 struct GroupLayout {
     // Cholesky: packed L then the 8 x 8 diagonal-block inverses; LU: the square Gram (+ unused)
-    static constexpr size_t ls_floats = SOLVER == 0   ? (cg_split_rows(SOLVER, FP) ? 128 * CG_SROW : 0)
+    static constexpr size_t ls_floats = SOLVER == 0   ? (cg_split_rows(SOLVER, FP) ? cgq_floats(FP) : 0)
                                         : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
                                         : SOLVER == 3 ? cgtc_tile_floats(FP)
                                                       : GroupSmem<FP>::ls_floats + 8 * FP;
@@ -138,7 +137,7 @@ inline int fp_of(int f) {
 constexpr size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
     const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
-    return solver == 0   ? (cg_split_rows(solver, fp) ? 128 * (size_t)CG_SROW : 0) + vec
+    return solver == 0   ? (cg_split_rows(solver, fp) ? (size_t)cgq_floats(fp) : 0) + vec
            : solver == 1 ? tri + 8 * (size_t)fp + vec
            : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + vec + 31) / 32 * 32
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
@@ -424,32 +423,6 @@ __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, uint32_t bcol, float
         : "memory");
 }
 
-// The split CG row at FP = 112: columns 56..111 (for shared memory) and columns 0..55 with b
-// (column bcol), one round trip each.
-__device__ __forceinline__ void tmem_ld_tail56(uint32_t taddr, float (&t)[56]) {
-    asm volatile(
-        "{\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%56];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39}, [%57];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55}, [%58];\n\t"
-        "tcgen05.wait::ld.sync.aligned;\n\t}"
-        : "=f"(t[0]), "=f"(t[1]), "=f"(t[2]), "=f"(t[3]), "=f"(t[4]), "=f"(t[5]), "=f"(t[6]), "=f"(t[7]), "=f"(t[8]), "=f"(t[9]), "=f"(t[10]), "=f"(t[11]), "=f"(t[12]), "=f"(t[13]), "=f"(t[14]), "=f"(t[15]), "=f"(t[16]), "=f"(t[17]), "=f"(t[18]), "=f"(t[19]), "=f"(t[20]), "=f"(t[21]), "=f"(t[22]), "=f"(t[23]), "=f"(t[24]), "=f"(t[25]), "=f"(t[26]), "=f"(t[27]), "=f"(t[28]), "=f"(t[29]), "=f"(t[30]), "=f"(t[31]), "=f"(t[32]), "=f"(t[33]), "=f"(t[34]), "=f"(t[35]), "=f"(t[36]), "=f"(t[37]), "=f"(t[38]), "=f"(t[39]), "=f"(t[40]), "=f"(t[41]), "=f"(t[42]), "=f"(t[43]), "=f"(t[44]), "=f"(t[45]), "=f"(t[46]), "=f"(t[47]), "=f"(t[48]), "=f"(t[49]), "=f"(t[50]), "=f"(t[51]), "=f"(t[52]), "=f"(t[53]), "=f"(t[54]), "=f"(t[55])
-        : "r"(taddr + 56u), "r"(taddr + 64u), "r"(taddr + 96u)
-        : "memory");
-}
-__device__ __forceinline__ void tmem_ld_head56(uint32_t taddr, uint32_t bcol, float (&a)[56], float &b) {
-    asm volatile(
-        "{\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%57];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%58];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%48,%49,%50,%51,%52,%53,%54,%55}, [%59];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%56}, [%60];\n\t"
-        "tcgen05.wait::ld.sync.aligned;\n\t}"
-        : "=f"(a[0]), "=f"(a[1]), "=f"(a[2]), "=f"(a[3]), "=f"(a[4]), "=f"(a[5]), "=f"(a[6]), "=f"(a[7]), "=f"(a[8]), "=f"(a[9]), "=f"(a[10]), "=f"(a[11]), "=f"(a[12]), "=f"(a[13]), "=f"(a[14]), "=f"(a[15]), "=f"(a[16]), "=f"(a[17]), "=f"(a[18]), "=f"(a[19]), "=f"(a[20]), "=f"(a[21]), "=f"(a[22]), "=f"(a[23]), "=f"(a[24]), "=f"(a[25]), "=f"(a[26]), "=f"(a[27]), "=f"(a[28]), "=f"(a[29]), "=f"(a[30]), "=f"(a[31]), "=f"(a[32]), "=f"(a[33]), "=f"(a[34]), "=f"(a[35]), "=f"(a[36]), "=f"(a[37]), "=f"(a[38]), "=f"(a[39]), "=f"(a[40]), "=f"(a[41]), "=f"(a[42]), "=f"(a[43]), "=f"(a[44]), "=f"(a[45]), "=f"(a[46]), "=f"(a[47]), "=f"(a[48]), "=f"(a[49]), "=f"(a[50]), "=f"(a[51]), "=f"(a[52]), "=f"(a[53]), "=f"(a[54]), "=f"(a[55]), "=f"(b)
-        : "r"(taddr + 0u), "r"(taddr + 32u), "r"(taddr + 48u), "r"(taddr + bcol)
-        : "memory");
-}
-
 // ------------------------------------------------------------------------------------- kernels
 
 // sum_j D[i][j] x_j re-read from TMEM in 16-column chunks (FP64 products and sums when WIDE)
@@ -716,38 +689,58 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // (xw, the CG warm start, was loaded by the caller as soon as the row was known)
         if constexpr (cg_split_rows(SOLVER, FP)) {
-            // columns CG_R.. of the row go to this thread's shared-memory row, the rest stays in
-            // registers; the accumulator is released once both halves are read
-            float *srow = Ls + i * CG_SROW;
+            // quad-blocked rows (cg_quad): chunk k (columns 16k..16k+15) of row i is cut into
+            // four float4, one per lane of the quad; rows 4a+2, 4a+3 go straight to their
+            // owners' shared slots, rows 4a, 4a+1 move across the quad by shuffles (lane c
+            // takes rows 4a and 4a+1 from lanes c^m, m = 1, 2, 3, or keeps its own)
+            constexpr int NK = FP / 16;
+            static_assert(CGQ_SLOT * 4 * 2 * NK == cgq_floats(FP), "quad slot layout");
+            float4 *sa = reinterpret_cast<float4 *>(Ls);
+            float4 ar[2][NK];
+            const int c = i & 3;
+            const int qa = i & ~3;
             {
-                float t[FP - CG_R];
-                tmem_ld_tail56(tb, t);
+                float b0, b1;
+                tmem_ld2(tb + p.ng, b0, b1);
+                bi = i < f ? b0 : 0.f;
+            }
 #pragma unroll
-                for (int j = 0; j < FP - CG_R; ++j) {
-                    const int col = CG_R + j;
-                    float v = col < p.ng && i < f ? t[j] : 0.f;
-                    if (col == i) v = i < f ? v + reg : 1.f;  // identity on the padded rows
-                    t[j] = v;
+            for (int k = 0; k < NK; ++k) {
+                float v[16];
+                if (16 * k < p.ng) {  // warp-uniform
+                    tmem_ld16(tb + 16 * k, v);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = 0.f;
                 }
 #pragma unroll
-                for (int j = 0; j < FP - CG_R; j += 4)
-                    *reinterpret_cast<float4 *>(srow + j) = make_float4(t[j], t[j + 1], t[j + 2], t[j + 3]);
-            }
-            float ar[CG_R];
-            float b;
-            tmem_ld_head56(tb, (uint32_t)p.ng, ar, b);
+                for (int j = 0; j < 16; ++j) {
+                    const int col = 16 * k + j;
+                    float x = col < p.ng && i < f ? v[j] : 0.f;
+                    if (col == i) x = i < f ? x + reg : 1.f;  // identity on the padded rows
+                    v[j] = x;
+                }
+                float4 V[4];
 #pragma unroll
-            for (int j = 0; j < CG_R; ++j) {
-                float v = j < p.ng && i < f ? ar[j] : 0.f;
-                if (j == i) v = i < f ? v + reg : 1.f;
-                ar[j] = v;
+                for (int g4 = 0; g4 < 4; ++g4)
+                    V[g4] = make_float4(v[4 * g4], v[4 * g4 + 1], v[4 * g4 + 2], v[4 * g4 + 3]);
+                if (c >= 2) {
+#pragma unroll
+                    for (int g4 = 0; g4 < 4; ++g4)
+                        sa[(2 * k + c - 2) * CGQ_SLOT + qa + g4] = V[g4];
+                }
+                const float4 s1 = c == 0 ? V[1] : V[0];
+                const float4 s2 = c == 0 ? V[2] : V[3];
+                const float4 s3 = c == 0 ? V[3] : V[2];
+                const float4 r1 = shfl_xor4(s1, 1), r2 = shfl_xor4(s2, 2), r3 = shfl_xor4(s3, 3);
+                ar[0][k] = c == 0 ? V[0] : c == 1 ? r1 : c == 2 ? r2 : r3;
+                ar[1][k] = c == 0 ? r1 : c == 1 ? V[1] : c == 2 ? r3 : r2;
             }
-            bi = i < f ? b : 0.f;
             tc_fence_before();
-            gs.sync();
+            gs.sync();  // (also orders the slots' stores before the first product)
             if (et == 0) mbar_arrive(release);
             released = true;
-            xi = cg_split<FP, CG_R>(ar, srow, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
+            xi = cg_quad<NK>(ar, sa, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
         } else {
         // the Gram row (columns < ng) and b (column ng) in one or two TMEM round trips
         float a[FP];
@@ -1046,11 +1039,12 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             };
             for (;;) {
                 const int s = it % NSTAGE;
+                // (every writer of the stage's operands fenced its generic stores into the async
+                // proxy before it arrived: the acquire of this wait is all the MMA needs)
                 if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort)) {
                     ok = false;
                     break;
                 }
-                fence_async_smem();
                 tc_fence_after();
                 const Meta m = smeta[s];
                 if (m.row < 0) {  // end of work: one end marker per solver warpgroup
