@@ -20,9 +20,9 @@ constexpr int MAX_NSTAGE = 8;
 // Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
 // gathered bytes in flight per SM); the LU scratch leaves room for five stages, and so does the
 // Cholesky's except at FP = 112, where four factor groups share the SM.  The tensor-core CG keeps
-// only a 7 KB operand tile per group.
+// only a 7 KB operand tile per group: eight stages at FP <= 112 (measured 1-2% faster than six).
 __host__ __device__ constexpr int nstage_of(int solver, int fp) {
-    return solver == 3 ? 6
+    return solver == 3 ? (fp <= 112 ? 8 : 6)
            : solver == 0 ? (fp == 112 ? 4 : 8)
                          : (solver == 1 && fp == 112) ? 4 : 5;
 }
