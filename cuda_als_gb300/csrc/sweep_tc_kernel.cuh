@@ -28,7 +28,7 @@ __host__ __device__ constexpr int nstage_of(int solver, int fp) {
 }
 // CG at FP = 112 quad-blocks its rows (cg_quad): half of a row's values in registers, half in
 // shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups fit an SM.
-__host__ __device__ constexpr bool cg_split_rows(int solver, int fp) { return solver == 0 && fp == 112; }
+__host__ __device__ constexpr bool cg_quad_rows(int solver, int fp) { return solver == 0 && fp == 112; }
 __host__ __device__ constexpr int cgq_floats(int fp) { return 2 * (fp / 16) * 130 * 4; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
@@ -60,15 +60,16 @@ __host__ __device__ constexpr int cgtc_tile_floats(int fp) { return (fp / 8) * 6
 // ng = 128) and solver groups: CG and LU read their row out of TMEM into registers at once and
 // release the buffer, so the MMA fills the next row while they solve; their register-resident
 // rows allow two groups per SM.  A Cholesky group keeps its buffer until refinement has re-read
-// A, and its factor lives in shared memory: one group per buffer; so does the split-row CG, and
-// the tensor-core CG, whose products read A from the buffer until the solve ends.
+// A, and its factor lives in shared memory: one group per buffer; so does the quad-blocked CG
+// (half of each row in shared memory), and the tensor-core CG, whose products read A from the
+// buffer until the solve ends.
 __host__ __device__ constexpr int nbuf_of(int fp) { return fp == 128 ? 2 : 4; }
 __host__ __device__ constexpr int nepi_of(int solver, int fp) {
-    return solver == 1 || solver == 3 || cg_split_rows(solver, fp) ? nbuf_of(fp) : nbuf_of(fp) / 2;
+    return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(fp) : nbuf_of(fp) / 2;
 }
 // Gather warps: as many as the registers the solvers need allow.  A launch's registers are
 // shared out per four warps, so above 640 threads a thread keeps 80 and at 640 it keeps 96: the
-// tensor-core CG (about 60 a thread) takes six, the other solvers two (the split-row CG and the
+// tensor-core CG (about 60 a thread) takes six, the other solvers two (the quad-blocked CG and the
 // Cholesky factor need 96 and 84 at four groups).
 __host__ __device__ constexpr int ngather_of(int solver, int fp) {
     return solver == 3 ? 6 : 2;
@@ -112,7 +113,7 @@ struct GroupSmem {
 template <int FP, int SOLVER>
 struct GroupLayout {
     // Cholesky: packed L then the 8 x 8 diagonal-block inverses; LU: the square Gram (+ unused)
-    static constexpr size_t ls_floats = SOLVER == 0   ? (cg_split_rows(SOLVER, FP) ? cgq_floats(FP) : 0)
+    static constexpr size_t ls_floats = SOLVER == 0   ? (cg_quad_rows(SOLVER, FP) ? cgq_floats(FP) : 0)
                                         : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
                                         : SOLVER == 3 ? cgtc_tile_floats(FP)
                                                       : GroupSmem<FP>::ls_floats + 8 * FP;
@@ -137,7 +138,7 @@ inline int fp_of(int f) {
 constexpr size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
     const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
-    return solver == 0   ? (cg_split_rows(solver, fp) ? (size_t)cgq_floats(fp) : 0) + vec
+    return solver == 0   ? (cg_quad_rows(solver, fp) ? (size_t)cgq_floats(fp) : 0) + vec
            : solver == 1 ? tri + 8 * (size_t)fp + vec
            : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + vec + 31) / 32 * 32
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
@@ -688,7 +689,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     } else {
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
         // (xw, the CG warm start, was loaded by the caller as soon as the row was known)
-        if constexpr (cg_split_rows(SOLVER, FP)) {
+        if constexpr (cg_quad_rows(SOLVER, FP)) {
             // quad-blocked rows (cg_quad): chunk k (columns 16k..16k+15) of row i is cut into
             // four float4, one per lane of the quad; rows 4a+2, 4a+3 go straight to their
             // owners' shared slots, rows 4a, 4a+1 move across the quad by shuffles (lane c
