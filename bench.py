@@ -5,7 +5,9 @@ One step = one ALS epoch (U half-sweep over the CSR, then V half-sweep over the 
 library's sweep, inputs resident in HBM; by default the BF16 tensor-core sweep with the per-bucket
 Cholesky/CG autotuner (ALS_SOLVE_AUTO), epochs replayed from the captured CUDA graph.  The timed
 region is K steps bracketed by a barrier and a device synchronize, timed with CUDA events on the
-stream the library launches on.  The inputs (an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors)
+stream the library launches on; the K epochs are one `iterate(K)` call, which replays them back to
+back (a call per epoch would add the call's own synchronize and status read-back, host time the
+device spends idle, to every epoch).  The inputs (an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors)
 are far larger than the 129 MB L2, so no flush is needed between steps.
 
 The same run also measures, on the same data:
@@ -17,9 +19,10 @@ The same run also measures, on the same data:
   * cpu_baseline: the same ALS update on the host cores (the oracle in FP32, OpenMP over rows),
     timed on a random row sample of each side and scaled to a full epoch.
 
-`--impl reference` times the reference's algorithm on the CPU instead (the reference itself is
-a CUDA program whose removed cuSPARSE call and closed-library dependencies keep it from being
-built here; its restatement in oracle/ is what runs), on the same workload and metric.
+`--impl reference` times the reference's algorithm on the CPU instead (the reference program
+itself cannot be built: its host code calls a cuSPARSE function CUDA 11 removed; its restatement
+in oracle/ is what runs), on the same workload and metric.  The reference's own CUDA kernels, built
+from its sources into cubins, are timed on the GPU separately by `python -m oracle.ref_cuda_epoch`.
 
 Multi-GPU: rows of a half-sweep shard naturally, but every box of this setup has one GPU, so
 `--gpus N` runs N independent replicas (weak scaling); the line reports the slowest replica.
@@ -315,8 +318,7 @@ def run_ours(args):
         barrier()
         with torch.cuda.stream(stream):
             e0.record(stream)
-        for _ in range(steps):
-            mdl.iterate(1)
+        mdl.iterate(steps)
         with torch.cuda.stream(stream):
             e1.record(stream)
         barrier()

@@ -4,6 +4,8 @@
  *
  * Each function cites the reference file:line it restates.  FP64 is the oracle precision;
  * the FP32 variant (use_fp32) is the same ALS update in float, used as the CPU baseline.
+ * Pinned to the reference's own CUDA path (its Gram and CG kernels built from its sources, the
+ * cuBLAS batched LU it calls) through outputs of that path on workload 1 (tests/test_refpin.py).
  */
 #include "als_oracle.h"
 

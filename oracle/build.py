@@ -63,6 +63,44 @@ def build_ref(verbose: bool = False) -> Path | None:
     return REF_OUT
 
 
+# The reference's own Gram and CG kernels, compiled from its sources where they lie into
+# device-only cubins for sm_103a: `calculate_vtvs` (als_model.cu:91-167, the Gram of its SIMPLE
+# vtvs type) and `updateXWithCGKernel` (cumf_als_cg/cg.cu:37-232).  A cubin holds GPU code only,
+# so it is built here and loaded on the GPU machine (oracle/refkernels.py), where the reference tree
+# is absent.  als_model.cu's host code calls cusparseScsrmm2, which CUDA 11 removed; that call
+# is defined away on the command line: it sits in host code that no cubin contains.
+REF_CUBINS = {
+    "model": (REF_SRC / "als_model.cu", HERE / "_ref" / "ref_model.cubin"),
+    "cg": (REF_SRC / "cumf_als_cg" / "cg.cu", HERE / "_ref" / "ref_cg.cubin"),
+}
+
+
+def build_ref_cubins(verbose: bool = False) -> dict[str, Path]:
+    """Build oracle/_ref/ref_{model,cg}.cubin where the reference sources are present; return
+    the cubins that exist."""
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    out = {}
+    for key, (src, dst) in REF_CUBINS.items():
+        if src.exists() and Path(nvcc).exists() and not (
+                dst.exists() and src.stat().st_mtime <= dst.stat().st_mtime):
+            dst.parent.mkdir(exist_ok=True)
+            tmp = dst.with_name(dst.name + ".tmp")
+            cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                   f"-I{REF_SRC}", f"-I{REF_SRC / 'cumf_als_cg'}",
+                   "-DcusparseScsrmm2(...)=CUSPARSE_STATUS_NOT_SUPPORTED",
+                   "-diag-suppress", "177", str(src), "-o", str(tmp)]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"reference cubin build failed for {src.name}:\n{r.stderr}")
+            os.replace(tmp, dst)
+        if dst.exists():
+            out[key] = dst
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose=True))
     print(build_ref(verbose=True))
+    print(build_ref_cubins(verbose=True))
