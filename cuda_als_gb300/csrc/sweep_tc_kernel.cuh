@@ -18,12 +18,13 @@ namespace tcg {
 constexpr int KC = 64;                       // ratings per stage
 constexpr int MAX_NSTAGE = 8;
 // Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
-// gathered bytes in flight per SM); the LU scratch leaves room for five stages, and so does the
-// Cholesky's except at FP = 112, where four factor groups share the SM.  The tensor-core CG keeps
-// only a 7 KB operand tile per group: eight stages at FP <= 112 (measured 1-2% faster than six).
+// gathered bytes in flight per SM; five stages beside the quad-blocked rows at FP = 112); the LU
+// scratch leaves room for five stages, and so does the Cholesky's except at FP = 112, where four
+// factor groups share the SM.  The tensor-core CG keeps only a 7 KB operand tile per group: eight
+// stages at FP <= 112 (measured 1-2% faster than six).
 __host__ __device__ constexpr int nstage_of(int solver, int fp) {
     return solver == 3 ? (fp <= 112 ? 8 : 6)
-           : solver == 0 ? (fp == 112 ? 4 : 8)
+           : solver == 0 ? (fp == 112 ? 5 : 8)
                          : (solver == 1 && fp == 112) ? 4 : 5;
 }
 // CG at FP = 112 quad-blocks its rows (cg_quad): half of a row's values in registers, half in
@@ -117,10 +118,12 @@ struct GroupLayout {
                                         : SOLVER == 1 ? TriLayout<FP>::floats + 8 * FP
                                         : SOLVER == 3 ? cgtc_tile_floats(FP)
                                                       : GroupSmem<FP>::ls_floats + 8 * FP;
-    // (the tensor-core CG's groups start on 128-byte boundaries: its tile is an MMA operand)
+    // (the tensor-core CG's groups start on 128-byte boundaries: its tile is an MMA operand;
+    // the quad-blocked CG needs no vectors past the reduction ring)
     static constexpr size_t floats =
         SOLVER == 3 ? (ls_floats + 2 * FP + 16 + 5 * 128 + 64 + 31) / 32 * 32
-                    : ls_floats + 2 * FP + 16 + 5 * 128 + 64;
+        : cg_quad_rows(SOLVER, FP) ? ls_floats + 2 * FP + 16
+                                   : ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
 struct Geometry {
@@ -138,7 +141,7 @@ inline int fp_of(int f) {
 constexpr size_t group_floats(int fp, int solver) {
     const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
     const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
-    return solver == 0   ? (cg_quad_rows(solver, fp) ? (size_t)cgq_floats(fp) : 0) + vec
+    return solver == 0   ? (cg_quad_rows(solver, fp) ? (size_t)cgq_floats(fp) + 2 * (size_t)fp + 16 : vec)
            : solver == 1 ? tri + 8 * (size_t)fp + vec
            : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + vec + 31) / 32 * 32
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
