@@ -53,7 +53,9 @@ def test_reference_gram_kernel_is_the_oracle_gram():
         assert _rel(G[u], A) < 1e-6
 
 
-@pytest.mark.parametrize("solve,f", [(ca.SOLVE_TYPE.LU, 10), (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 32)])
+@pytest.mark.parametrize("solve,f", [(ca.SOLVE_TYPE.LU, 10), (ca.SOLVE_TYPE.LU, 32),
+                                     (ca.SOLVE_TYPE.LU, 64), (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 32),
+                                     (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 64)])
 def test_fp32_half_sweep_matches_the_reference(solve, f):
     tr, te, m, n, lam, csr, test = _workload1()
     U0, V0 = O.init_factors(m, n, f)

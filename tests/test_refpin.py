@@ -22,6 +22,7 @@ import pytest
 
 import cuda_als_gb300 as ca
 from oracle import oracle as O
+from oracle import refkernels as RK
 
 FIX = Path(__file__).with_name("golden") / "refkernels_workload1.npz"
 
@@ -76,3 +77,11 @@ def test_oracle_cg_reproduces_the_reference(ref):
     U, V, _ = O.train(m, n, f, lam, 10, csr, csc, solve=O.CG_FP32, fp32=True)
     assert _rel(V, d["cg_V"]) < 2e-3
     assert abs(O.rmse(*test, U, V) - float(d["cg_rmse"])) < 1e-4
+
+
+def test_reference_launches_stay_within_the_kernels_int_offsets():
+    """The reference's kernels offset the Gram buffer by blockIdx.x * f * f in int: every launch of
+    them (oracle/refkernels.py) covers at most batch_rows(f) rows, the most that stay below 2^31."""
+    for f in (10, 32, 64, 100, 128):
+        b = RK.batch_rows(f)
+        assert (b - 1) * f * f + f * f - 1 < 2**31 <= (b + 1) * f * f
