@@ -63,6 +63,8 @@ def parse_args():
                         "the FP16-Gram CG, its products on the tensor core)")
     p.add_argument("--iters", type=int, default=None, help="iterations for the RMSE comparison")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-rows", action="store_true",
+                   help="skip the per-row timings (init, LU epoch, RMSE, adjoint, degree order)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-compare", action="store_true",
                    help="skip the plain-FP32 Cholesky and BF16 Cholesky+refinement comparisons")
@@ -152,6 +154,52 @@ def load_traffic(args, side, prec_name):
                     and sv == args.solve and sd == side):
                 return float(b)
     return None
+
+
+def measure_rows(model, make, time_epochs, tr, te, info, peak_hbm):
+    """Times of the path's other rows on this workload, through the public API (host wall time
+    around synchronous calls, after a warm call; median of 5 where a call is short):
+    A2 init, A6 the LU sweep (the tensor-core Gram with the reference's LU semantics), A9 the
+    test RMSE (FP64, fixed order; algorithmic bytes = 12 B per test rating + its two factor rows),
+    A10 the user half-sweep adjoint on the test set as held-out data, A12 the degree order of the
+    rows.  The transpose (A11) is `stage_ms.transpose`."""
+    import torch
+
+    import cuda_als_gb300 as ca
+
+    f = info["f"]
+
+    def wall(fn, reps=5):
+        fn()
+        out = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            out.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(out)
+
+    res = {}
+    res["A2_init_ms"] = round(wall(model.init_factors), 3)
+    model.iterate(3)
+    nt = int(te.val_cnt)
+    rmse_ms = wall(model.rsme_test)
+    rmse_bytes = nt * (12 + 8 * f)
+    res["A9_rmse_test"] = {"ms": round(rmse_ms, 3), "algorithmic_bytes": rmse_bytes,
+                           "GB_s": round(rmse_bytes / (rmse_ms * 1e-3) / 1e9, 1),
+                           "frac_of_hbm": round(rmse_bytes / (rmse_ms * 1e-3) / 1e9 / peak_hbm, 4)}
+    held = (te.h_coo_row_idxs, te.h_csr_coo_col_idxs, te.h_csr_coo_vals)
+    res["A10_adjoint_ms"] = round(wall(lambda: model.user_halfsweep_adjoint(*held), reps=2), 3)
+    res["A12_degree_order_ms"] = round(wall(lambda: ca.degree_order(tr.h_csr_row_ptrs)), 3)
+    lu = make(ca.PRECISION.BF16, ca.SOLVE_TYPE.LU)
+    lu.init_factors()
+    lu.iterate(3)
+    res["A6_lu_epoch_ms"] = round(time_epochs(lu, 2), 3)
+    lu.close()
+    res["note"] = ("host wall time of synchronous API calls (A10 and A12 include their host "
+                   "copies: the held-out set and dL/dY, the row pointers and the order)")
+    return res
 
 
 def dist_setup(args):
@@ -402,6 +450,12 @@ def run_ours(args):
                "d2h_bytes_per_step": d2h, "device_event_ms": round(ev, 3),
                "host_wall_ms": round(wall, 3)}
 
+    # ---- the other rows of the path, each through the public API on the same workload (after the
+    # measured sweep: none of this is inside its timed region)
+    rows = None
+    if not args.no_rows and rank == 0:
+        rows = measure_rows(model, make, time_epochs, tr, te, info, peak_hbm)
+
     # ---- roofline of the dominant kernel (the U half-sweep's contraction)
     gram_u, rhs_u, solve_u = flops_per_half(nnz, m, f)
     gram_v, rhs_v, solve_v = flops_per_half(nnz, n, f)
@@ -437,7 +491,7 @@ def run_ours(args):
         "stage_ms": {k: round(v, 3) for k, v in stage.items()},
         "test_rmse_after_iters": rmse, "iters": iters,
         "fp32_plain": fp32, "bf16_cholesky_refined": chol, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "clocks": clocks, "gpu_launches": launches,
+        "clocks": clocks, "gpu_launches": launches, "rows": rows,
         "flagged_rows": counters["flagged_rows"],
     }
     line["plan"] = plan
