@@ -21,8 +21,9 @@ index the Gram buffer with int (`blockIdx.x * f * f`), so every launch covers at
 passes the batch offset, als_model.cu:1891-1896): one launch of 480,189 rows at f = 100 would
 write below the buffer.
 
-Only tests/ import this module.  The cubins are built where the reference tree is present and
-travel with the repository; without them `available()` is False.
+Only tests/ and the timing script beside it (oracle/ref_cuda_epoch.py) import this module.  The
+cubins are built where the reference tree is present and travel with the repository; without them
+`available()` is False.
 """
 from __future__ import annotations
 
