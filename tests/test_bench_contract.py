@@ -42,3 +42,21 @@ def test_reference_arm_runs_on_rank_zero_only():
     r = _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_roofline_traffic_comes_from_the_committed_capture():
+    """The GPU arm's roofline.traffic is read from profiles/dram_traffic.txt for the default
+    workload and plan; other workloads report null rather than a borrowed figure."""
+    import argparse
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    a = argparse.Namespace(config=3, scale=1.0, solve="auto")
+    u, v = bench.load_traffic(a, "U", "bf16"), bench.load_traffic(a, "V", "bf16")
+    assert u is not None and v is not None
+    # the U half's DRAM bytes stay near its algorithmic floor (8 B per rating + 800 B per row)
+    floor = 8 * 98_600_426 + 800 * 480_189
+    assert 0.9 * floor < u < 1.3 * floor
+    assert bench.load_traffic(argparse.Namespace(config=2, scale=1.0, solve="auto"), "U",
+                              "bf16") is None
