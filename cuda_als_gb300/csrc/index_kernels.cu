@@ -12,6 +12,7 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <utility>
 #include <string>
 
 #include "internal.h"
@@ -516,20 +517,21 @@ cudaError_t count_bad_entries(int64_t nnz, const int32_t *idx, int32_t limit, co
 // CSR -> CSC without any allocation, for callers that may not allocate device memory.
 //
 // Some callers cannot call cudaMalloc (or have torch or any other allocator do it for them):
-// code that runs while a stream is being captured into a CUDA graph in the global capture mode,
-// where an allocation invalidates the capture; plug-ins hosted by an engine that owns all device
-// memory and forbids allocations inside its callbacks; and latency-critical loops that must not
-// synchronise on the allocator.  For them the transpose's scratch lives in one file-scope device
-// array of NOALLOC_SCRATCH_BYTES (16 MiB), which every GPU that loads this library holds until the
-// process exits.  That bounds the input to about 590,000 ratings; larger inputs are rejected with
+// plug-ins hosted by an engine that owns all device memory and forbids allocations inside its
+// callbacks, and latency-critical loops that must not synchronise on the allocator.  For them the
+// transpose's scratch lives in one file-scope device array of NOALLOC_SCRATCH_BYTES (16 MiB),
+// which every GPU that loads this library holds until the process exits.  The compact transpose
+// needs 28 bytes per rating plus 1 KiB per 4,096 ratings (its radix histograms), each array
+// rounded up to 256 bytes, which admits at most 593,856 ratings; larger inputs are rejected with
 // ALS_ERR_INVALID_ARG before anything runs.
 //
 // In host code the array's name is only a host-side stand-in, so the device address is looked up
-// once per device with cudaGetSymbolAddress (with that device current) on the first call made on
-// it; make that first call before any stream capture begins.  Every call shares the one array:
-// calls whose work overlaps on the GPU (different streams, or several threads) race on it and
-// must be serialised by the caller.  The transpose writes every scratch word before it reads it,
-// so no clearing is needed between calls.
+// with cudaGetSymbolAddress (with the device current) on the first call made in each CUDA
+// context, and looked up again when the device's context changes (after cudaDeviceReset the
+// module reloads at another address).  Every call shares the one array: calls whose work
+// overlaps on the GPU (different streams, or several threads) race on it and must be serialised
+// by the caller.  The transpose writes every scratch word before it reads it, so no clearing is
+// needed between calls.
 // ---------------------------------------------------------------------------------------------
 
 namespace {
@@ -541,6 +543,30 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 std::mutex g_noalloc_mu;
 void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+unsigned long long g_noalloc_ctx[NOALLOC_MAX_DEVICES] = {};  // cuCtxGetId of the lookup's context
+
+// The unique id of the calling thread's current CUDA context (cuCtxGetCurrent + cuCtxGetId
+// through the runtime's driver entry points; no link against libcuda); 0 if unavailable.
+unsigned long long current_context_id() {
+    typedef int (*GetCurrentFn)(void **);
+    typedef int (*GetIdFn)(void *, unsigned long long *);
+    static const std::pair<GetCurrentFn, GetIdFn> fns = []() {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) !=
+                cudaSuccess || qa != cudaDriverEntryPointSuccess)
+            a = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) !=
+                cudaSuccess || qb != cudaDriverEntryPointSuccess)
+            b = nullptr;
+        return std::make_pair(reinterpret_cast<GetCurrentFn>(a), reinterpret_cast<GetIdFn>(b));
+    }();
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (!fns.first || !fns.second || fns.first(&ctx) != 0 || !ctx || fns.second(ctx, &id) != 0)
+        return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -571,8 +597,11 @@ extern "C" als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int
         return set_global_error(ALS_ERR_UNSUPPORTED, "device ordinal beyond 63");
     void *scratch = nullptr;
     {
+        // cudaGetDevice made the device's primary context current if it was not yet
+        const unsigned long long ctx = current_context_id();
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {  // set-up, once per device, with that device current
+        if (!g_noalloc_addr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
+            // set-up, once per device and context, with that device current
             void *addr = nullptr;
             e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
             if (e != cudaSuccess || !addr)
@@ -580,6 +609,7 @@ extern "C" als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int
                                         std::string("cudaGetSymbolAddress: ") +
                                             cudaGetErrorString(e));
             g_noalloc_addr[dev] = addr;
+            g_noalloc_ctx[dev] = ctx;
         }
         scratch = g_noalloc_addr[dev];
     }

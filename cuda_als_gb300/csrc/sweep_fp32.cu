@@ -12,10 +12,16 @@
 // the Gram lives in shared memory only.
 //
 // Layout.  The gathered panel Z (KC ratings x FP features, FP32) carries the rating itself as
-// feature f, so the (f+1) x (f+1) Gram of [Y | r] holds A_u in its leading f x f block and b_u in
-// row f.  Each thread owns a 4 x 8 register tile of the lower block triangle (8 x 8 blocks, split
-// in two), so the FMA work is the lower triangle only.  After the last chunk the tiles are
-// stored to shared memory (stride FP+1, conflict-free column walks) and the CTA solves in place.
+// feature f.  Each thread owns a 4 x 8 register tile of the lower block triangle of the Gram
+// (8 x 8 blocks, split in two), so the FMA work is the lower triangle only; each Gram entry is
+// one sequential FMA chain over the row's ratings, in rating order (the order of the reference's
+// calculate_vtvs, als_model.cu:137-155).  The right-hand side is summed apart, more accurately:
+// thread j sums r_k y_kj over each KC-rating chunk and adds the chunk sums with compensated
+// (Kahan) addition, so b_u carries about one rounding instead of the n_u of a sequential sum.
+// (An FP32 sequential right-hand side costs ALS up to 4x in accuracy against FP64 after ten
+// iterations at f = 100-128: its error meets the Gram's condition number in every solve.)  After
+// the last chunk the tiles are stored to shared memory (stride FP+1, conflict-free column walks)
+// and the CTA solves in place.
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -77,6 +83,7 @@ __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, con
     for (int p = 0; p < 4; ++p)
 #pragma unroll
         for (int c = 0; c < 8; ++c) acc[p][c] = 0.f;
+    float bsum = 0.f, bcomp = 0.f;  // b_tid: compensated sum of the chunk sums (tid < f)
 
     for (int base = beg; base < end; base += KC) {
         const int cnt = min(KC, end - base);
@@ -109,6 +116,14 @@ __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, con
                     for (int c = 0; c < 8; ++c) acc[p][c] = fmaf(ar[p], cr[c], acc[p][c]);
             }
         }
+        if (tid < f) {
+            float cs = 0.f;  // this chunk's r_k y_k,tid, sequential
+            for (int k = 0; k < cnt; ++k) cs = fmaf(Z[k * FP + f], Z[k * FP + tid], cs);
+            const float y = cs - bcomp;  // Kahan step (no products: nothing to contract)
+            const float t = bsum + y;
+            bcomp = (t - bsum) - y;
+            bsum = t;
+        }
         __syncthreads();
     }
 
@@ -121,10 +136,10 @@ __global__ void __launch_bounds__(1024) sweep_fp32_kernel(const SweepArgs a, con
     }
     __syncthreads();
     const float reg = (float)nu * a.lambda;  // items_cnt * lambda (als_model.cu:157-159)
-    for (int i = tid; i < f; i += blockDim.x) {
-        G[i * GS + i] += reg;
-        vb[i] = G[f * GS + i];
-        vx[i] = xo[i];
+    if (tid < f) {  // (the launch has at least f threads)
+        G[tid * GS + tid] += reg;
+        vb[tid] = bsum;
+        vx[tid] = xo[tid];
     }
     __syncthreads();
 
@@ -166,6 +181,7 @@ cudaError_t launch_sweep_fp32(const SweepArgs &a, cudaStream_t st, int *launches
     const int n = a.row_end - a.row_begin;
     if (n <= 0) return cudaSuccess;
     const int FP = fp_of(a.f);
+    if (nt_of(FP) < a.f) return cudaErrorInvalidConfiguration;  // thread j owns b_j
     const size_t smem = smem_of(FP);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sweep_fp32_kernel,

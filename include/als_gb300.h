@@ -278,13 +278,13 @@ als_status als_csr_to_csc_device(const als_csr_view *csr, int32_t *col_ptrs, int
                                  float *vals, void *stream);
 
 /* The same stable transpose without allocating anything: for callers that may not allocate
- * device memory (a stream being captured into a CUDA graph in the global capture mode, a plug-in
- * inside an engine that owns all device memory, an allocation-free latency-critical loop).  No
- * counterpart in the reference.  Scratch is a fixed 16 MiB device array inside this library, so
- * inputs up to about 590,000 ratings are accepted and larger ones rejected with
- * ALS_ERR_INVALID_ARG.  The first call on a device looks the array up (make it before any stream
- * capture); all calls share the array, so calls that overlap on the GPU race and must be
- * serialised by the caller.  DEVICE pointers, enqueued on `stream`. */
+ * device memory (a plug-in inside an engine that owns all device memory, an allocation-free
+ * latency-critical loop).  No counterpart in the reference.  Scratch is a fixed 16 MiB device
+ * array inside this library; the transpose needs 28 bytes per rating plus 1 KiB per 4,096
+ * ratings, each array rounded up to 256 bytes, so at most 593,856 ratings are accepted and larger
+ * inputs are rejected with ALS_ERR_INVALID_ARG.  The first call in each CUDA context looks the
+ * array up (again after a device reset); all calls share the array, so calls that overlap on the
+ * GPU race and must be serialised by the caller.  DEVICE pointers, enqueued on `stream`. */
 als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int32_t *col_ptrs,
                                          int32_t *row_idxs, float *vals, void *stream);
 

@@ -147,8 +147,16 @@ def gram(ptr, idx, Y, f, lam):
     return vtvs.view(rows, f, f).transpose(1, 2).cpu().numpy()
 
 
-def half_sweep(ptr, idx, val, Y, X, f, lam, solve="lu"):
-    """One half-sweep as the reference runs it; returns the new X (rows x f, FP32)."""
+def m_batches_for(rows: int, f: int) -> int:
+    """Fewest batches whose first (largest) batch keeps the Gram kernel's int offsets in range."""
+    return max(1, -(-rows // batch_rows(f)))
+
+
+def half_sweep(ptr, idx, val, Y, X, f, lam, solve="lu", m_batches=None):
+    """One half-sweep as the reference runs it; returns the new X (rows x f, FP32).  Rows go in
+    `m_batches` contiguous batches split as als_model.cu:1891-1896 splits them (first batches
+    (rows - 1) / m_batches + 1 rows, the last the rest), each with its Gram launch at the batch
+    offset and its own batched solve; by default the fewest batches the int offsets allow."""
     import torch
 
     dev = torch.device("cuda")
@@ -159,43 +167,53 @@ def half_sweep(ptr, idx, val, Y, X, f, lam, solve="lu"):
     d_Y = torch.as_tensor(np.ascontiguousarray(Y, np.float32), device=dev)
     R = torch.sparse_csr_tensor(d_ptr, d_idx, d_val, size=(rows, n))
     B = (R @ d_Y).contiguous()  # rows x f: b_u contiguous per row (the reference's VTRT)
-    assert rows <= batch_rows(f), "one launch: the kernel's int Gram offsets"
-    vtvs = torch.zeros(rows * f * f, dtype=torch.float32, device=dev)
-    _launch(_cuda()[2]["model"], rows, f, 0, [vtvs, d_ptr, d_idx, float(lam), rows, f, d_Y, 0])
-    if solve == "lu":
-        lib, h = _cublas()
-        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-        _check(lib.cublasSetStream_v2(h, stream), "cublasSetStream")
-        a_ptrs = torch.arange(rows, dtype=torch.int64, device=dev) * (f * f * 4) + vtvs.data_ptr()
-        b_ptrs = torch.arange(rows, dtype=torch.int64, device=dev) * (f * 4) + B.data_ptr()
-        infos = torch.zeros(rows, dtype=torch.int32, device=dev)
-        vp = C.c_void_p
-        _check(lib.cublasSgetrfBatched(h, C.c_int(f), vp(a_ptrs.data_ptr()), C.c_int(f), None,
-                                       vp(infos.data_ptr()), C.c_int(rows)), "cublasSgetrfBatched")
-        info = C.c_int(0)
-        _check(lib.cublasSgetrsBatched(h, C.c_int(0), C.c_int(f), C.c_int(1), vp(a_ptrs.data_ptr()),
-                                       C.c_int(f), None, vp(b_ptrs.data_ptr()), C.c_int(f),
-                                       C.byref(info), C.c_int(rows)), "cublasSgetrsBatched")
-        torch.cuda.synchronize()
-        return B.cpu().numpy()
+    nb = m_batches or m_batches_for(rows, f)
+    first = (rows - 1) // nb + 1
+    assert first <= batch_rows(f), "one launch: the kernel's int Gram offsets"
+    vtvs = torch.zeros(first * f * f, dtype=torch.float32, device=dev)
     if solve == "cg":
         assert f % 32 == 0 and f <= 64, "the reference CG kernel needs whole warps (f = 32, 64)"
         d_X = torch.as_tensor(np.ascontiguousarray(X, np.float32), device=dev).clone()
-        _launch(_cuda()[2]["cg"], rows, f, (4 * f + 4) * 4,
-                [vtvs, d_X, B, rows, f, float(CG_ITER)])
-        torch.cuda.synchronize()
-        return d_X.cpu().numpy()
-    raise ValueError(solve)
+    elif solve != "lu":
+        raise ValueError(solve)
+    for k in range(nb):
+        off = k * first
+        bs = min(first, rows - off)
+        if bs <= 0:
+            break
+        vtvs.zero_()
+        _launch(_cuda()[2]["model"], bs, f, 0, [vtvs, d_ptr, d_idx, float(lam), rows, f, d_Y, off])
+        if solve == "lu":
+            lib, h = _cublas()
+            stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+            _check(lib.cublasSetStream_v2(h, stream), "cublasSetStream")
+            a_ptrs = torch.arange(bs, dtype=torch.int64, device=dev) * (f * f * 4) + vtvs.data_ptr()
+            b_ptrs = (torch.arange(bs, dtype=torch.int64, device=dev) * (f * 4) + B.data_ptr() +
+                      off * f * 4)
+            infos = torch.zeros(bs, dtype=torch.int32, device=dev)
+            vp = C.c_void_p
+            _check(lib.cublasSgetrfBatched(h, C.c_int(f), vp(a_ptrs.data_ptr()), C.c_int(f), None,
+                                           vp(infos.data_ptr()), C.c_int(bs)), "cublasSgetrfBatched")
+            info = C.c_int(0)
+            _check(lib.cublasSgetrsBatched(h, C.c_int(0), C.c_int(f), C.c_int(1),
+                                           vp(a_ptrs.data_ptr()), C.c_int(f), None,
+                                           vp(b_ptrs.data_ptr()), C.c_int(f), C.byref(info),
+                                           C.c_int(bs)), "cublasSgetrsBatched")
+        else:
+            _launch(_cuda()[2]["cg"], bs, f, (4 * f + 4) * 4,
+                    [vtvs, d_X[off:off + bs], B[off:off + bs], bs, f, float(CG_ITER)])
+    torch.cuda.synchronize()
+    return (B if solve == "lu" else d_X).cpu().numpy()
 
 
-def train(m, n, f, lam, iters, csr, csc, solve="lu"):
+def train(m, n, f, lam, iters, csr, csc, solve="lu", m_batches=None, n_batches=None):
     """srand(0) init, then iters x (U over the CSR, V over the CSC) -> (U, V)."""
     from . import oracle as O
 
     U, V = O.init_factors(m, n, f)
     for _ in range(iters):
-        U = half_sweep(csr[0], csr[1], csr[2], V, U, f, lam, solve)
-        V = half_sweep(csc[0], csc[1], csc[2], U, V, f, lam, solve)
+        U = half_sweep(csr[0], csr[1], csr[2], V, U, f, lam, solve, m_batches)
+        V = half_sweep(csc[0], csc[1], csc[2], U, V, f, lam, solve, n_batches)
     return U, V
 
 

@@ -101,3 +101,67 @@ def test_reference_epoch_timer_runs_the_reference_lu_path():
     V = RK.half_sweep(*csc, U, V0, f, lam, "lu")
     assert _rel(ep.X[0].cpu().numpy(), U) < 1e-5
     assert _rel(ep.X[1].cpu().numpy(), V) < 1e-5
+
+
+# Scaled workloads 3, 4 and 5 at their own f (100, 128, 128): the FP32 path against the
+# reference's LU path, whose Gram runs on CUDA cores at these f (its tensor-core kernels stop at
+# f = 80 / 112).  Scale 0.1 / 0.1 / 0.25: 48,019 x 1,777 (986k ratings), its transpose, and
+# 70,807 x 14,525 (1.5M ratings).
+WORKLOAD_CASES = [(3, 0.1), (4, 0.1), (5, 0.25)]
+
+
+def _scaled(config, scale):
+    tr, te, info = ca.synth_generate(config, scale=scale)
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    csr = (tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, tr.h_csr_coo_vals)
+    test = (te.h_coo_row_idxs, te.h_csr_coo_col_idxs, te.h_csr_coo_vals)
+    return tr, te, m, n, f, lam, csr, test
+
+
+@pytest.mark.parametrize("config,scale", WORKLOAD_CASES)
+def test_fp32_half_sweeps_match_the_reference_at_the_workload_f(config, scale):
+    """One U and one V half-sweep from the srand(0) init, each side from the same inputs as the
+    reference's (its V from the reference's U), rows in the reference's m_batches split."""
+    tr, te, m, n, f, lam, csr, test = _scaled(config, scale)
+    csc = O.csr_to_csc(m, n, *csr)
+    U0, V0 = O.init_factors(m, n, f)
+    Ur = RK.half_sweep(*csr, V0, U0, f, lam, "lu", m_batches=3)
+    Vr = RK.half_sweep(*csc, Ur, V0, f, lam, "lu", m_batches=2)
+    with _fp32_model(tr, te, f, lam, 1, ca.SOLVE_TYPE.LU) as mdl:
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(0)
+        U, _ = mdl.get_factors()
+        mdl.set_factors(Ur, V0)
+        mdl.half_sweep(1)
+        _, V = mdl.get_factors()
+    assert _rel(U, Ur) < TOL
+    assert _rel(V, Vr) < TOL
+
+
+@pytest.mark.parametrize("config,scale", WORKLOAD_CASES)
+def test_fp32_training_matches_the_reference_at_the_workload_f(config, scale):
+    """10 iterations from the srand(0) init at the workload's f and lambda, with the FP64 oracle's
+    training (exact arithmetic on the same inputs) as the arbiter.
+
+    * The library's factors lie within 1e-4 (relative) of the FP64 training.
+    * They lie within 1e-4 of the reference's, or, where the reference's own FP32 result is
+      farther from FP64 than 1e-4 / 2, within twice that distance.  Ten rounds of ALS amplify
+      each half-sweep's rounding (the solves meet Grams of condition number ~10^2-10^3), so two
+      FP32 implementations drift apart by the sum of their distances from exact arithmetic.
+      Measured on workload 4 (f = 128): reference to FP64 1.07e-4 (U), library to FP64 4.1e-5,
+      library to reference 1.0e-4 (U) and 1.9e-4 (V); on workloads 3 and 5 every distance is
+      below 6e-5.
+    * Test RMSE within 1e-4 of the reference's."""
+    tr, te, m, n, f, lam, csr, test = _scaled(config, scale)
+    csc = O.csr_to_csc(m, n, *csr)
+    Ur, Vr = RK.train(m, n, f, lam, 10, csr, csc, "lu", m_batches=3, n_batches=2)
+    Ue, Ve, _ = O.train(m, n, f, lam, 10, csr, csc, solve=O.CHOLESKY)  # FP64
+    with _fp32_model(tr, te, f, lam, 10, ca.SOLVE_TYPE.LU) as mdl:
+        mdl.train()
+        U, V = mdl.h_UT, mdl.h_VT
+        rmse = mdl.rsme_test()
+        assert mdl.counters()["flagged_rows"] == 0
+    for X, Xr, Xe in ((U, Ur, Ue), (V, Vr, Ve)):
+        assert _rel(X, Xe) < TOL
+        assert _rel(X, Xr) < max(TOL, 2 * _rel(Xr, Xe))
+    assert abs(rmse - O.rmse(*test, Ur, Vr)) < TOL

@@ -1,9 +1,7 @@
 """The allocation-free transpose entry point (als_csr_to_csc_device_noalloc).
 
-It is for callers that may not allocate device memory: code running while a stream is captured
-into a CUDA graph in the global capture mode (an allocation there invalidates the capture), a
-plug-in hosted by an engine that owns all device memory, or a latency-critical loop that must not
-wait on an allocator.  It keeps its scratch in one fixed array inside the library instead.  Its
+It is for callers that may not allocate device memory: a plug-in hosted by an engine that owns
+all device memory, or a latency-critical loop that must not wait on an allocator.  It keeps its scratch in one fixed array inside the library instead.  Its
 output must be identical to the allocating entry point's (als_csr_to_csc_device) on every call:
 this is integer and permutation work, so the comparison is bit-exact.  The file is named so that
 pytest collects it last.
