@@ -1,28 +1,33 @@
 #!/usr/bin/env python
 """ALS epoch benchmark on the 480,189 x 17,770, 100M-rating workload (f = 100, lambda = 0.048).
 
-One step = one ALS epoch (U half-sweep over the CSR, then V half-sweep over the CSC) of the
-library's sweep, inputs resident in HBM; by default the BF16 tensor-core sweep with the per-bucket
-Cholesky/CG autotuner (ALS_SOLVE_AUTO), epochs replayed from the captured CUDA graph.  The timed
-region is K steps bracketed by a barrier and a device synchronize, timed with CUDA events on the
-stream the library launches on; the K epochs are one `iterate(K)` call, which replays them back to
-back (a call per epoch would add the call's own synchronize and status read-back, host time the
-device spends idle, to every epoch).  The inputs (an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors)
-are far larger than the 129 MB L2, so no flush is needed between steps.
+One step = one configured training run of the library's sweep: als_init_factors (the srand(0)
+init) and the configured 10 ALS epochs (U half-sweep over the CSR, then V half-sweep over the CSC),
+inputs resident in HBM; by default the BF16 tensor-core sweep with the per-bucket Cholesky/CG
+autotuner (ALS_SOLVE_AUTO), epochs replayed from the captured CUDA graph.  `value` is ms per
+epoch: the CUDA-event time of the K runs' 10-epoch `iterate` calls on the stream the library
+launches on, over 10 K; the test RMSE reported is that of the timed runs (they are bit-identical:
+each starts from the same init).  The first run on a fresh handle also holds the autotuner's
+tuning sweep and the graph's capture and instantiation; it is a warm-up run, timed and reported
+apart (`cold_run`).  The inputs (an 0.8 GB CSR, a 0.8 GB CSC and 0.2 GB of factors) are far larger
+than the 129 MB L2, so no flush is needed between steps.
 
 The same run also measures, on the same data:
   * the plain-FP32 Cholesky sweep (the comparison of the metric) and the BF16 Cholesky sweep with
-    one refinement step, epoch ms and test RMSE after the configured 10 iterations;
-  * e2e: the same epoch through the C ABI with HOST buffers: each step re-uploads the ratings
-    from pinned memory (als_reload: H2D, validation, GPU transpose, degree orders), runs the
-    epoch and reads back both factor tables and the test RMSE;
+    one refinement step: one warm-up and one timed configured run each, epoch ms and test RMSE;
+  * e2e: the same training run through the C ABI with HOST buffers: each step re-uploads the
+    ratings from pinned memory (als_reload: H2D, validation, GPU transpose, degree orders),
+    initialises, runs the 10 epochs and reads back both factor tables and the test RMSE;
+  * the half-sweep times averaged over the epochs of one configured run (the roofline's kernel);
   * cpu_baseline: the same ALS update on the host cores (the oracle in FP32, OpenMP over rows),
     timed on a random row sample of each side and scaled to a full epoch.
 
-`--impl reference` times the reference's algorithm on the CPU instead (the reference program
-itself cannot be built: its host code calls a cuSPARSE function CUDA 11 removed; its restatement
-in oracle/ is what runs), on the same workload and metric.  The reference's own CUDA kernels, built
-from its sources into cubins, are timed on the GPU separately by `python -m oracle.ref_cuda_epoch`.
+`--impl reference` times the reference's algorithm on the CPU instead, whole epochs (the reference
+program itself cannot be built: its host code calls a cuSPARSE function CUDA 11 removed; its
+restatement in oracle/ is what runs), on the same workload and metric, with the workload made by
+the oracle-side build of the generator (the product library is not loaded).  Where a GPU is
+present it also times the reference's own CUDA path (its Gram kernel built from its sources +
+cuBLAS batched LU, oracle/refkernels.py) and reports it as `reference_cuda`.
 
 Multi-GPU: rows of a half-sweep shard naturally, but every box of this setup has one GPU, so
 `--gpus N` runs N independent replicas (weak scaling); the line reports the slowest replica.
@@ -51,8 +56,8 @@ UNIT = "ms/epoch"
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=40,
-                   help="timed epochs (40 x ~25 ms: long enough for several clock samples)")
+    p.add_argument("--steps", type=int, default=5,
+                   help="timed training runs of the configured iterations each")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
@@ -262,55 +267,87 @@ def cpu_epoch_estimate(tr, info, seconds, seed=0):
                       f"{spent:.1f} s of host time, scaled by rows to one epoch"}
 
 
+def reference_cuda_epoch(csr, csc, info, epochs=3):
+    """The reference's own CUDA path on this GPU (oracle/refkernels.py Epoch: its shared-memory
+    FP32 Gram kernel built from its sources, cuBLAS batched LU without pivoting, the right-hand
+    side by cuSPARSE SpMM, rows in batches as its m_batches loop splits them): one warm-up epoch,
+    then `epochs` epochs timed with CUDA events (LU has no early exit: every epoch costs the
+    same).  None without a GPU or without the reference's cubins."""
+    try:
+        import torch
+    except ImportError:
+        return None
+    from oracle import refkernels as RK
+
+    if not torch.cuda.is_available() or not RK.available():
+        return None
+    m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
+    ep = RK.Epoch(m, n, f, lam, csr, csc)
+    ep.epoch()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(epochs):
+        ep.epoch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / epochs
+    del ep
+    torch.cuda.empty_cache()
+    return {"ms_per_epoch": round(ms, 3), "epochs_timed": epochs,
+            "path": "reference CUDA kernels (calculate_vtvs_smem_row_major, als_model.cu:169-241) "
+                    "+ cuBLAS getrf/getrsBatched without pivoting + cuSPARSE SpMM, FP32"}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
     from oracle import oracle as O
+    from oracle import synth
 
-    tr, te, info = workload(args, pinned=False)
+    (ptr, idx, val), _, info = synth.generate(args.config, scale=args.scale)
     m, n, f, lam = info["m"], info["n"], info["f"], info["lambda"]
-    ptr, idx, val = tr.h_csr_row_ptrs, tr.h_csr_coo_col_idxs, tr.h_csr_coo_vals
     cptr, cidx, cval = O.csr_to_csc(m, n, ptr, idx, val)
     U, V = O.init_factors(m, n, f)
     rng = np.random.default_rng(1)
-    frac = 0.002
-    budget = max(10.0, 150.0 / max(1, args.steps + args.warmup))  # whole run: a few minutes
 
-    def step(frac):
-        su = np.sort(rng.choice(m, size=max(1, int(m * frac)), replace=False)).astype(np.int32)
-        sv = np.sort(rng.choice(n, size=max(1, int(n * frac)), replace=False)).astype(np.int32)
+    def epoch(frac=None):
+        """One epoch of the host ALS update (FP32, OpenMP over rows): every row of both sides,
+        or a random `frac` of them (the untimed warm-up)."""
+        su = sv = None
+        if frac is not None:
+            su = np.sort(rng.choice(m, size=max(1, int(m * frac)), replace=False)).astype(np.int32)
+            sv = np.sort(rng.choice(n, size=max(1, int(n * frac)), replace=False)).astype(np.int32)
         t0 = time.perf_counter()
         O.half_sweep(ptr, idx, val, V, U, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=su)
-        t1 = time.perf_counter()
         O.half_sweep(cptr, cidx, cval, U, V, f, lam, solve=O.CHOLESKY, fp32=True, rows_subset=sv)
-        t2 = time.perf_counter()
-        return ((t1 - t0) * m / len(su) + (t2 - t1) * n / len(sv)) * 1e3, t2 - t0, len(su), len(sv)
+        return (time.perf_counter() - t0) * 1e3
 
-    _, spent, _, _ = step(frac)
-    frac = min(1.0, frac * max(1.0, budget / max(spent, 1e-3)))
     for _ in range(args.warmup):
-        step(frac * 0.25)
-    vals = []
-    for _ in range(args.steps):
-        v, spent, nu, nv = step(frac)
-        vals.append(v)
+        epoch(0.01)
+    t0 = time.perf_counter()
+    vals = [epoch() for _ in range(args.steps)]
+    wall = time.perf_counter() - t0
     value = float(np.mean(vals))
     cores = O.max_threads()
-    sample = (f"per step: random {nu} of {m} rows (U side) and {nv} of {n} rows (V side), "
-              f"scaled by rows to one epoch")
+    ref_cuda = reference_cuda_epoch((ptr, idx, val), (cptr, cidx, cval), info)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": f"synthetic (seeded, workload {args.config} shapes)",
-        "config": config_dict(args, info, "fp32-host"),
+        "config": dict(config_dict(args, info, "fp32-host"),
+                       step="one whole epoch (every row of both sides)"),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": f"whole epochs: all {m} + {n} rows per step, "
+                                                   f"{args.steps} steps in {wall:.1f} s"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_cuda": ref_cuda,
         "note": "the reference's sweep restated on the host (oracle/, FP32, OpenMP over rows, "
-                "per-row Gram + RHS + Cholesky); the reference program itself is CUDA-only",
+                "per-row Gram + RHS + Cholesky); the reference program itself is CUDA-only. "
+                "reference_cuda: the reference's own CUDA path on this GPU, for context",
     }
     print(json.dumps(line), flush=True)
 
@@ -373,7 +410,21 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def time_epochs(mdl, steps, sampler=None):
+    def run(mdl):
+        """One configured training run: init (host srand(0) + upload, outside the events), then
+        the `iters` epochs between CUDA events on the library's stream -> device ms."""
+        mdl.init_factors()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        mdl.iterate(iters)  # synchronous: returns once the epochs ran
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    def time_epochs(mdl, steps):
+        """Epoch ms of `steps` back-to-back epochs from the current state (the LU row)."""
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         with torch.cuda.stream(stream):
@@ -384,23 +435,31 @@ def run_ours(args):
         barrier()
         return e0.elapsed_time(e1) / steps
 
-    def rmse_after(mdl, k):
-        mdl.init_factors()
-        mdl.iterate(k)
-        return mdl.rsme_test()
-
     peak_hbm, peak_bf16, peak_src = load_peaks()
 
-    # ---- the measured precision
+    # ---- the measured sweep: a cold run (tuning sweep + graph capture), warm-up runs, K timed runs
     model = make(prec)
-    model.init_factors()
-    for _ in range(max(3, args.warmup)):
-        model.iterate(1)
+    t0 = time.perf_counter()
+    cold_dev = run(model)
+    cold = {"ms_per_epoch": round(cold_dev / iters, 3),
+            "host_wall_ms": round((time.perf_counter() - t0) * 1e3, 3),
+            "note": "the first run on a fresh handle: includes the autotuner's tuning sweep "
+                    "(every bucket solved with each candidate solver, timed) and the capture and "
+                    "instantiation of the epoch's CUDA graph"}
+    warm = max(3, args.warmup)
+    for _ in range(warm - 1):
+        run(model)
+    runs = []
+    barrier()
     with ClockSampler(local) as clk:
-        ms = time_epochs(model, args.steps)
+        for _ in range(args.steps):
+            runs.append(run(model))
+        barrier()
     clocks = clk.summary()
-    stage = model.stage_ms()
+    ms = sum(runs) / (args.steps * iters)
+    rmse = model.rsme_test()  # the test RMSE of the timed runs (each from the same init)
     counters = model.counters()
+    launches_per_epoch = int(counters["launches"])
     plan = {side: [dict(b, **t) for b, t in zip(model.plan(k), model.tuning(k) or
                                                 [{}] * len(model.plan(k)))]
             for k, side in ((0, "U"), (1, "V"))}
@@ -408,21 +467,34 @@ def run_ours(args):
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    rmse = rmse_after(model, iters)
+
+    # ---- the half-sweep times averaged over the epochs of one configured run (one call per
+    # epoch: the library reads its per-half events after each), and the same run's RMSE
+    model.init_factors()
+    halves = {"U": [], "V": [], "quantise": []}
+    for _ in range(iters):
+        model.iterate(1)
+        st = model.stage_ms()
+        for k in halves:
+            halves[k].append(st[k])
+    stage = {k: float(np.mean(v)) for k, v in halves.items()}
+    stage["transpose"] = model.stage_ms()["transpose"]
+    deterministic = model.rsme_test() == rmse
 
     # ---- the metric's comparison: plain FP32 Cholesky on the same data; and the BF16 Cholesky
-    # sweep with one refinement step (FP64 residual on ill-conditioned rows), the configuration
-    # the >= 3x target names, when the measured sweep is not already that
+    # sweep with one refinement step (FP64 residual on rows above the condition threshold), the
+    # configuration the >= 3x target names, when the measured sweep is not already that; one
+    # warm-up and one timed configured run each
     def compare(precision, how):
         ref = make(precision, how)
-        ref.init_factors()
-        ref.iterate(3)
-        cms = time_epochs(ref, max(2, min(args.steps, 3)))
-        cst = ref.stage_ms()
-        crmse = rmse_after(ref, iters)
+        run(ref)
+        cms = run(ref) / iters
+        crmse = ref.rsme_test()
+        cc = ref.counters()
         ref.close()
-        return cms, {"ms_per_epoch": round(cms, 3), "U_ms": round(cst["U"], 3),
-                     "V_ms": round(cst["V"], 3), "test_rmse_after_iters": crmse}
+        return cms, {"ms_per_epoch": round(cms, 3), "test_rmse_after_iters": crmse,
+                     "fp64_refined_rows": int(cc["fp64_refined_rows"]),
+                     "flagged_rows": int(cc["flagged_rows"])}
 
     fp32 = chol = None
     if not args.no_compare and prec != ca.PRECISION.FP32:
@@ -435,32 +507,38 @@ def run_ours(args):
                         rmse_delta_vs_fp32=abs(chol["test_rmse_after_iters"] -
                                                fp32["test_rmse_after_iters"]))
 
-    # ---- e2e through the C ABI with host buffers
+    # ---- e2e: the same training run through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        U = np.empty((m, f), np.float32)
-        V = np.empty((n, f), np.float32)
+        # page-locked read-back buffers (the owners stay referenced: freeing one would leave
+        # its array pointing at unmapped memory)
+        pinned = [ca._Pinned(m * f, np.float32), ca._Pinned(n * f, np.float32)]
+        U, V = pinned[0].array.reshape(m, f), pinned[1].array.reshape(n, f)
         model.reload(tr, te)  # warm
         barrier()
         t0 = time.perf_counter()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             e0.record(stream)
+        e2e_rmse = None
         for _ in range(args.steps):
-            model.reload(tr, te)
-            model.iterate(1)
-            model.get_factors(U, V)
-            model.rsme_test()
+            model.reload(tr, te)     # H2D: CSR + test COO, GPU transpose, degree orders
+            model.init_factors()     # srand(0) on the host, V uploaded
+            model.iterate(iters)
+            model.get_factors(U, V)  # D2H: both factor tables
+            e2e_rmse = model.rsme_test()
         with torch.cuda.stream(stream):
             e1.record(stream)
         barrier()
-        wall = (time.perf_counter() - t0) * 1e3 / args.steps
-        ev = e0.elapsed_time(e1) / args.steps
-        h2d = 4 * (m + 1 + 2 * nnz) + 12 * nnz_test
+        wall = (time.perf_counter() - t0) * 1e3 / (args.steps * iters)
+        ev = e0.elapsed_time(e1) / (args.steps * iters)
+        h2d = 4 * (m + 1 + 2 * nnz) + 12 * nnz_test + 4 * n * f
         d2h = 4 * (m + n) * f + 8
         e2e = {"value": round(max(ev, wall), 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "device_event_ms": round(ev, 3),
-               "host_wall_ms": round(wall, 3)}
+               "host_wall_ms": round(wall, 3), "test_rmse": e2e_rmse,
+               "step": f"als_reload + als_init_factors + {iters} epochs + both factor tables "
+                       f"read back + test RMSE; value per epoch"}
 
     # ---- the other rows of the path, each through the public API on the same workload (after the
     # measured sweep: none of this is inside its timed region)
@@ -468,11 +546,11 @@ def run_ours(args):
     if not args.no_rows and rank == 0:
         rows = measure_rows(model, make, time_epochs, tr, te, info, peak_hbm)
 
-    # ---- roofline of the dominant kernel (the U half-sweep's contraction)
+    # ---- roofline of the dominant kernel (the U half-sweep: quantise + one launch per bucket)
     gram_u, rhs_u, solve_u = flops_per_half(nnz, m, f)
     gram_v, rhs_v, solve_v = flops_per_half(nnz, n, f)
-    dom_ms = stage["U"] if stage["U"] >= stage["V"] else stage["V"]
     dom_side = "U" if stage["U"] >= stage["V"] else "V"
+    dom_ms = stage[dom_side]
     dom_flops = gram_u + rhs_u
     achieved = dom_flops / (dom_ms * 1e-3) / 1e12
     gram_tflops = (gram_u + gram_v) / (ms * 1e-3) / 1e12
@@ -480,9 +558,12 @@ def run_ours(args):
     roofline = {"bound": "tensor", "achieved": round(achieved, 3), "peak": peak_bf16,
                 "unit": "TFLOP/s", "frac": round(achieved / peak_bf16, 4),
                 "traffic": traffic,
+                "traffic_source": "recorded: profiles/dram_traffic.txt (ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum of this workload's half-sweep launches), "
+                                  "not measured in this run" if traffic is not None else None,
                 "kernel": f"fused half-sweep ({dom_side} side: BF16 quantise + one sweep_tc_kernel "
                           f"launch per nnz bucket), Gram+RHS flops nnz*f*(f+1)+2*nnz*f over its "
-                          f"CUDA-event time",
+                          f"CUDA-event time averaged over the {iters} epochs of a configured run",
                 "peak_source": f"bf16 dense, {peak_src}"}
     if prec == ca.PRECISION.FP32:
         roofline["note"] = "FP32 path runs on CUDA cores: the fraction is of the bf16 tensor peak"
@@ -491,20 +572,23 @@ def run_ours(args):
     if not args.no_cpu and rank == 0:
         cpu = cpu_epoch_estimate(tr, info, args.cpu_seconds)
 
-    launches = int(counters["launches"]) * args.steps  # kernels per epoch (both halves) x steps
     line = {
         "metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 3),
+        "steps": args.steps, "warmup": warm, "ms_per_step": round(ms * iters, 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": prec_name, "data": f"synthetic (seeded, workload {args.config} shapes"
                                          + ("; Netflix stand-in)" if args.config == 3 else ")"),
-        "config": config_dict(args, info, prec_name),
+        "config": dict(config_dict(args, info, prec_name),
+                       step=f"one configured training run: als_init_factors + {iters} epochs"),
         "gram_tflops": round(gram_tflops, 3),
         "stage_ms": {k: round(v, 3) for k, v in stage.items()},
-        "test_rmse_after_iters": rmse, "iters": iters,
-        "fp32_plain": fp32, "bf16_cholesky_refined": chol, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "clocks": clocks, "gpu_launches": launches, "rows": rows,
-        "flagged_rows": counters["flagged_rows"],
+        "test_rmse_after_iters": rmse, "iters": iters, "rmse_reproduced": deterministic,
+        "cold_run": cold,
+        "fp32_plain": fp32, "bf16_cholesky_refined": chol, "roofline": roofline,
+        "cpu_baseline": cpu, "e2e": e2e,
+        "clocks": clocks, "gpu_launches": launches_per_epoch * iters * args.steps,
+        "rows": rows, "flagged_rows": int(counters["flagged_rows"]),
+        "fp64_refined_rows": int(counters["fp64_refined_rows"]),
     }
     line["plan"] = plan
     model.close()

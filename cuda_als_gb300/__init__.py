@@ -462,6 +462,10 @@ class als_model:
     def set_stream(self, stream_ptr: int | None):
         self._c(lib().als_set_stream(self._h, stream_ptr))
 
+    def set_wait_limit_ns(self, ns: int = 0):
+        """Bound of the sweep kernels' device waits in ns (0: the default, 10 s)."""
+        self._c(lib().als_set_wait_limit_ns(self._h, int(ns)))
+
     def stage_ms(self):
         out = (C.c_double * 4)()
         self._c(lib().als_get_stage_ms(self._h, out))
@@ -521,6 +525,28 @@ def csr_to_csc(rows: int, cols: int, row_ptrs, col_idxs, vals):
     cv = np.zeros(len(i), np.float32)
     _check(lib().als_csr_to_csc(C.byref(view), _ptr(cp), _ptr(ri), _ptr(cv)))
     return cp, ri, cv
+
+
+def coo_to_csr(rows: int, cols: int, row_idxs, col_idxs, vals, csc: bool = True):
+    """Rating triples -> (CSR (row_ptrs, col_idxs, vals), the row of each CSR entry, and the CSC
+    (col_ptrs, row_idxs, vals) or None), built on the GPU: scipy's coo_matrix(...).tocsr() /
+    .tocoo() / .tocsc() order, duplicates summed (FP64, rounded once to FP32)."""
+    r = np.ascontiguousarray(row_idxs, np.int32)
+    c = np.ascontiguousarray(col_idxs, np.int32)
+    v = np.ascontiguousarray(vals, np.float32)
+    view = CsrView(rows, cols, len(v), _ptr(r), _ptr(c), _ptr(v))
+    nz = len(v)
+    ptr = np.zeros(rows + 1, np.int32)
+    idx, val, crow = np.zeros(nz, np.int32), np.zeros(nz, np.float32), np.zeros(nz, np.int32)
+    cptr = np.zeros(cols + 1, np.int32) if csc else None
+    ridx = np.zeros(nz, np.int32) if csc else None
+    cval = np.zeros(nz, np.float32) if csc else None
+    out = C.c_int64()
+    _check(lib().als_coo_to_csr(C.byref(view), _ptr(ptr), _ptr(idx), _ptr(val), _ptr(crow),
+                                _ptr(cptr), _ptr(ridx), _ptr(cval), C.byref(out)))
+    k = out.value
+    return ((ptr, idx[:k], val[:k]), crow[:k],
+            (cptr, ridx[:k], cval[:k]) if csc else None)
 
 
 def degree_order(row_ptrs):

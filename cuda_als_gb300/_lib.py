@@ -82,12 +82,16 @@ def lib() -> C.CDLL:
         "als_get_stage_ms": ([H, C.POINTER(f64)], i32),
         "als_get_counters": ([H, C.POINTER(i64)], i32),
         "als_get_plan": ([H, i32, P, P, P, C.POINTER(i32)], i32),
+        "als_set_wait_limit_ns": ([H, u64], i32),
         "als_get_tuning": ([H, i32, P, P, P, P, P, C.POINTER(i32)], i32),
         "als_user_halfsweep_adjoint": ([H, C.POINTER(CooView), C.POINTER(f64), P,
                                         C.POINTER(f64)], i32),
         "als_csr_to_csc": ([C.POINTER(CsrView), P, P, P], i32),
         "als_csr_to_csc_device": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_csr_to_csc_device_noalloc": ([C.POINTER(CsrView), P, P, P, P], i32),
+        "als_coo_to_csr": ([C.POINTER(CooView), P, P, P, P, P, P, P, C.POINTER(i64)], i32),
+        "als_coo_to_csr_device": ([C.POINTER(CooView), P, P, P, P, P, P, P, C.POINTER(i64), P],
+                                  i32),
         "als_degree_order": ([i64, P, P], i32),
         "als_partition_rows": ([i64, P, i32, f64, P], i32),
         "als_log_create": ([C.c_char_p, C.POINTER(P)], i32),
@@ -122,9 +126,9 @@ EXPORTS = [
     "als_destroy", "als_last_error", "als_set_stream", "als_update_values", "als_reload", "als_init_factors",
     "als_iterate", "als_half_sweep", "als_train", "als_rmse_test", "als_rmse_train",
     "als_get_factors", "als_set_factors", "als_get_device_factors", "als_save_libmf",
-    "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan", "als_get_tuning",
+    "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan", "als_get_tuning", "als_set_wait_limit_ns",
     "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
-    "als_csr_to_csc_device_noalloc",
+    "als_csr_to_csc_device_noalloc", "als_coo_to_csr", "als_coo_to_csr_device",
     "als_degree_order", "als_partition_rows", "als_synth_shape", "als_synth_generate",
     "als_log_create", "als_log_destroy", "als_log_text", "als_log_event_started",
     "als_log_event_finished", "als_log_set_iters", "als_log_get_iters", "als_log_name",

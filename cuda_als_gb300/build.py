@@ -25,6 +25,7 @@ SOURCES = [
     "sweep.cpp",
     "synth.cpp",
     "index_kernels.cu",
+    "coo_build.cu",
     "sweep_fp32.cu",
     "sweep_tc.cu",
     "sweep_tc_fp32.cu",

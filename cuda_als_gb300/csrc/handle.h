@@ -53,6 +53,7 @@ struct als_handle {
     std::string last_error;
     double stage_ms[4] = {-1.0, -1.0, -1.0, -1.0};
     int64_t counters[3] = {0, 0, 0};
+    uint64_t wait_ns = 0;  // bound of the sweep kernels' device waits (0: the default, 10 s)
     std::vector<cudaEvent_t> events;
     cudaEvent_t ev_half[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     // one ALS epoch (U then V half-sweep) captured once the kernel plan is final, replayed by

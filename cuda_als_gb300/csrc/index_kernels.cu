@@ -499,6 +499,13 @@ __global__ void gather_f32_kernel(int64_t n, const int32_t *__restrict__ perm,
         dst[p] = src[perm[p]];
 }
 
+cudaError_t ptrs_from_sorted(int64_t n, int64_t nkeys, const int32_t *skeys, int32_t *ptr,
+                             cudaStream_t st) {
+    if (n <= 0) return cudaMemsetAsync(ptr, 0, sizeof(int32_t) * (size_t)(nkeys + 1), st);
+    col_ptrs_from_sorted_kernel<<<grid_for(n + 1, 256), 256, 0, st>>>(n, nkeys, skeys, ptr);
+    return cudaGetLastError();
+}
+
 cudaError_t gather_f32(int64_t n, const int32_t *perm, const float *src, float *dst,
                        cudaStream_t st) {
     if (n <= 0) return cudaSuccess;

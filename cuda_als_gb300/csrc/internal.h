@@ -51,6 +51,11 @@ cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int
                               int32_t *perm_out /* optional, nnz: CSC position -> CSR position */,
                               bool compact = false);
 
+// ptr[k] = first position of the ascending keys skeys[0..n) that is >= k, for k in [0, nkeys]
+// (the pointer array of sorted row or column indices).
+cudaError_t ptrs_from_sorted(int64_t n, int64_t nkeys, const int32_t *skeys, int32_t *ptr,
+                             cudaStream_t st);
+
 // dst[p] = src[perm[p]]
 cudaError_t gather_f32(int64_t n, const int32_t *perm, const float *src, float *dst,
                        cudaStream_t st);

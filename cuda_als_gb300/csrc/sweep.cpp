@@ -373,6 +373,13 @@ als_status check_sweep_flags(als_handle *h) {
     return ALS_OK;
 }
 
+extern "C" als_status als_set_wait_limit_ns(als_handle *h, uint64_t ns) {
+    if (!h) return set_global_error(ALS_ERR_INVALID_ARG, "null handle");
+    h->wait_ns = ns;
+    invalidate_graphs(h);  // the limit is a kernel argument captured in the epoch graph
+    return ALS_OK;
+}
+
 extern "C" als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t *kind,
                                    int32_t *solver, int32_t *nb) {
     if (!h || !nb || (side != 0 && side != 1))

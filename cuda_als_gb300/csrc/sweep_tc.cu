@@ -250,6 +250,7 @@ cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t 
     p.lambda = h->cfg.lambda;
     p.cg_tol = h->cfg.cg_tol;
     p.cond_threshold = h->cfg.cond_threshold;
+    p.wait_ns = h->wait_ns ? (unsigned long long)h->wait_ns : tcg::WAIT_NS;
     const int grid = (int)std::min<int64_t>(p.nrows, t->num_sms);
     if (grid <= 0) return cudaSuccess;
     switch (g.fp) {

@@ -79,7 +79,10 @@ __host__ __device__ constexpr int nthreads_of(int solver, int fp) {
     return 128 * nepi_of(solver, fp) + 32 * (2 + ngather_of(solver, fp));
 }
 
-constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s bound per wait
+// Bound of every spin-wait: the role waits use Params::wait_ns (the handle's limit, by default
+// WAIT_NS); the drains at the end of a CTA (in-flight MMAs, gathers, product chains) always get
+// WAIT_NS, so that a CTA that gave up still lets every copy it issued land before it exits.
+constexpr unsigned long long WAIT_NS = 10ull * 1000 * 1000 * 1000;  // 10 s
 
 struct Meta {  // per stage / per accumulator
     int32_t row;    // -1 = end of work
@@ -101,6 +104,7 @@ struct Params {
     int32_t nrows, zero_row, f, fst, ng, acc_stride, tmem_cols, nbuf, nepi, solve, cg_iters;
     int32_t refine_steps;
     float lambda, cg_tol, cond_threshold;
+    unsigned long long wait_ns;  // bound of the role waits (the drains keep WAIT_NS)
 };
 
 // Per-warpgroup shared scratch: L rows (or the FP32 Gram for the shared-memory LU) unless the
@@ -196,23 +200,26 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait; false on timeout or (when abort != nullptr) once another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
+// Bounded wait (`limit` ns, checked every 16 failed tries); false on timeout or (when
+// abort != nullptr) once another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort,
+                                          unsigned long long limit) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = now_ns();
     for (uint32_t i = 0;; ++i) {
         if (mbar_try(bar, parity)) return true;
-        if ((i & 255) == 255) {
+        if ((i & 15) == 15) {
             if (abort && *abort) return false;
-            if (now_ns() - t0 > WAIT_NS) return false;
+            if (now_ns() - t0 > limit) return false;
         }
     }
 }
 // Warp-uniform wait: lane 0 waits, the outcome is broadcast (no lane can diverge on a timeout),
 // and __syncwarp orders every lane's later memory accesses after lane 0's acquire.
-__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, volatile int *abort,
+                                               unsigned long long limit) {
     int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort) ? 1 : 0;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort, limit) ? 1 : 0;
     ok = __shfl_sync(0xffffffffu, ok, 0);
     __syncwarp();
     return ok != 0;
@@ -456,7 +463,8 @@ __device__ __forceinline__ int lane_of(int i) { return i & 31; }
 // The tensor-core CG's per-group state that outlives a row: the phase of its product barrier, and
 // whether the leader's last commit has not been seen to complete (drained before the CTA ends).
 struct CgTcState {
-    uint32_t phase = 0;
+    uint32_t phase = 0;       // product calls so far (the barrier phase each one waits for)
+    uint32_t committed = 0;   // the phase of the leader's last commit
     bool unconfirmed = false;
 };
 
@@ -499,8 +507,9 @@ __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, 
                                sdesc_plain(bt + 512u * kk, 256, 128), idesc, kk > 0 ? 1u : 0u);
             mma_commit(bar);
             st.unconfirmed = true;
+            st.committed = st.phase;
         }
-        const bool done = mbar_wait_warp(bar, st.phase & 1, abort);
+        const bool done = mbar_wait_warp(bar, st.phase & 1, abort, p.wait_ns);
         if (done) {
             if (et == 0) st.unconfirmed = false;
         } else {
@@ -932,7 +941,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 const unsigned long long t0 = now_ns();
                 for (uint32_t k = 0;; ++k) {
                     if ((uint32_t)*d > old) break;
-                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) {
+                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
                         r = 0;
                         break;
                     }
@@ -1036,7 +1045,8 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             auto take_buffer = [&]() -> bool {  // wait until accumulator acc_it % nbuf is free
                 buf = acc_it % nbuf;
                 const uint32_t use = acc_it / nbuf;
-                if (use >= 1 && !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort))
+                if (use >= 1 &&
+                    !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort, p.wait_ns))
                     return false;
                 tc_fence_after();
                 return true;
@@ -1045,7 +1055,8 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 const int s = it % NSTAGE;
                 // (every writer of the stage's operands fenced its generic stores into the async
                 // proxy before it arrived: the acquire of this wait is all the MMA needs)
-                if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort)) {
+                if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort,
+                               p.wait_ns)) {
                     ok = false;
                     break;
                 }
@@ -1088,7 +1099,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             }
             // drain: every MMA issued so far has completed before TMEM is released
             mma_commit(smem_u32(drain));
-            if (!mbar_wait(smem_u32(drain), 0, nullptr)) ok = false;
+            if (!mbar_wait(smem_u32(drain), 0, nullptr, WAIT_NS)) ok = false;
             if (!ok) {
                 *abort = 1;
                 atomicAdd(&p.flags[2], 1);
@@ -1107,7 +1118,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         bool ok = true;
         CgTcState cst;
         auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
-            if (et == 0) *okflag = mbar_wait(bar, parity, abort) ? 1 : 0;
+            if (et == 0) *okflag = mbar_wait(bar, parity, abort, p.wait_ns) ? 1 : 0;
             gs.sync();
             const bool r = *okflag != 0;
             gs.sync();
@@ -1142,8 +1153,9 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         }
         // a product chain whose completion was not seen (a wait ran out) finishes before TMEM is
         // released: after a failed wait the leader issues nothing more, so it is the last one
+        // (product calls after the abort commit nothing: wait for the last commit's phase)
         if (SOLVER == SOLVER_CGTC && et == 0 && cst.unconfirmed)
-            mbar_wait(smem_u32(&mvbar[g]), (cst.phase - 1) & 1, nullptr);
+            mbar_wait(smem_u32(&mvbar[g]), cst.committed & 1, nullptr, WAIT_NS);
         if (!ok) {  // (the tensor-core CG's waits are per warp: each failing warp counts)
             *abort = 1;
             if (SOLVER == SOLVER_CGTC ? lane == 0 : et == 0) atomicAdd(&p.flags[2], 1);
@@ -1172,7 +1184,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                         go = total > t ? 1 : 0;
                         break;
                     }
-                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) { go = -1; break; }
+                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
+                        go = -1;
+                        break;
+                    }
                 }
                 __threadfence_block();
             }
@@ -1194,7 +1209,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                     const unsigned long long t0 = now_ns();
                     for (uint32_t k = 0;; ++k) {
                         if (armed[s] >= (int)(t - NSTAGE)) break;
-                        if ((k & 255) == 255 && (*abort || now_ns() - t0 > WAIT_NS)) {
+                        if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
                             armed_ok = 0;
                             break;
                         }
@@ -1207,7 +1222,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 }
             }
             if (t >= NSTAGE &&
-                !mbar_wait_warp(smem_u32(&empty[s]), ((t / NSTAGE) - 1) & 1, abort)) {
+                !mbar_wait_warp(smem_u32(&empty[s]), ((t / NSTAGE) - 1) & 1, abort, p.wait_ns)) {
                 ok = false;
                 break;
             }
@@ -1272,7 +1287,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             __syncwarp();
             if constexpr (FUSED) {
                 // the stage's ratings into feature column ng, once its gathered rows have landed
-                if (!mbar_wait_warp(smem_u32(&full[s]), (t / NSTAGE) & 1, abort)) {
+                if (!mbar_wait_warp(smem_u32(&full[s]), (t / NSTAGE) & 1, abort, p.wait_ns)) {
                     ok = false;
                     break;
                 }
@@ -1297,7 +1312,8 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         if (h == 0 && lane == 0) {
             for (int u = 0; u < NSTAGE; ++u) {
                 const int a = armed[u];
-                if (a >= 0) mbar_wait(smem_u32(&full[u]), (uint32_t)(a / NSTAGE) & 1, nullptr);
+                if (a >= 0)
+                    mbar_wait(smem_u32(&full[u]), (uint32_t)(a / NSTAGE) & 1, nullptr, WAIT_NS);
             }
         }
         __syncwarp();

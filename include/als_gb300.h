@@ -235,6 +235,15 @@ als_status als_get_stage_ms(const als_handle *h, double out[4]);
  * residual was refined in FP64.  */
 als_status als_get_counters(const als_handle *h, int64_t out[3]);
 
+/* Bound, in nanoseconds, of every device-side wait of the tensor-core sweep kernels (a stage's
+ * gathered rows, a free accumulator, a finished Gram, a product on the tensor core); 0 restores
+ * the default of 10 s.  A wait that runs out makes its CTA stop taking rows, let every copy and
+ * MMA it issued finish (those drains keep the 10 s bound), free its tensor memory and return; the
+ * call then fails with ALS_ERR_TIMEOUT and the handle stays usable (the next call's status words
+ * start from zero).  A limit shorter than a healthy wait turns healthy sweeps into timeouts: it
+ * is a watchdog for a stuck device, and the way the timeout path is tested. */
+als_status als_set_wait_limit_ns(als_handle *h, uint64_t ns);
+
 /* The kernel choice per nnz bucket after autotuning: for bucket b, kind[b] (0 = FP32 SIMT,
  * 1 = BF16 tcgen05, 2 = FP8 tcgen05) and solver[b] (ALS_SOLVE_*).  nb in: capacity, out: count. */
 als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t *kind,
@@ -287,6 +296,29 @@ als_status als_csr_to_csc_device(const als_csr_view *csr, int32_t *col_ptrs, int
  * GPU race and must be serialised by the caller.  DEVICE pointers, enqueued on `stream`. */
 als_status als_csr_to_csc_device_noalloc(const als_csr_view *csr, int32_t *col_ptrs,
                                          int32_t *row_idxs, float *vals, void *stream);
+
+/* Rating triples -> the CSR, the row of every CSR entry and the CSC, built on the GPU.  Replaces
+ * the reference's offline scipy step (data/toy_data/prepare_toy_data.py:108-110, 147-150,
+ * 201-208; data/netflix/prepare_netflix_data.py:88-109): coo_matrix((vals, (rows, cols))) then
+ * .tocsr().tocoo() (R_train_coo.row.bin and the sorted test COO), .tocsr() (R_train_csr.*.bin)
+ * and .tocsc() (R_train_csc.*.bin), values cast to float32.  Entries end in (row, column) order;
+ * the triples of one cell (duplicates) are summed in FP64 and rounded once to FP32, which equals
+ * scipy's float64 sum + float32 cast whenever that sum is exact (any ratings on a common grid,
+ * such as star ratings).  Indices are 0-based; an index outside [0, rows) x [0, cols) fails with
+ * ALS_ERR_INVALID_ARG.  HOST pointers.  Output arrays hold coo->nnz entries (the upper bound);
+ * *nnz_out receives the count after summing duplicates (the CSR's row_ptrs[rows]).  coo_rows may
+ * be NULL; col_ptrs (cols + 1), row_idxs and csc_vals are all three given or all NULL. */
+als_status als_coo_to_csr(const als_coo_view *coo, int32_t *row_ptrs, int32_t *col_idxs,
+                          float *vals, int32_t *coo_rows, int32_t *col_ptrs, int32_t *row_idxs,
+                          float *csc_vals, int64_t *nnz_out);
+
+/* Same, DEVICE pointers, enqueued on `stream` (cudaStream_t as void*), scratch allocated with
+ * cudaMallocAsync on it; synchronous (the count after summing duplicates sizes the later
+ * launches and is returned in *nnz_out, host memory). */
+als_status als_coo_to_csr_device(const als_coo_view *coo, int32_t *row_ptrs, int32_t *col_idxs,
+                                 float *vals, int32_t *coo_rows, int32_t *col_ptrs,
+                                 int32_t *row_idxs, float *csc_vals, int64_t *nnz_out,
+                                 void *stream);
 
 /* Row order used by the persistent sweep: rows sorted by descending rating count, ties by
  * ascending row id (a stable sort).  Replaces contiguous m_batches/n_batches splitting

@@ -34,10 +34,42 @@ def build(verbose: bool = False) -> Path:
     return OUT
 
 
+# The workload generator (the library's synth.cpp, plain C++ with OpenMP) built on its own into
+# an oracle-side library, so that the CPU reference arm of the bench generates the same bytes
+# without loading the product library.  oracle/synth_errors.cpp stands in for the one library
+# function synth.cpp calls (the error recorder).
+SYNTH_SRC = HERE.parent / "cuda_als_gb300" / "csrc" / "synth.cpp"
+SYNTH_OUT = HERE / "_build" / f"libsynth-{platform.machine()}.so"
+
+
+def build_synth(verbose: bool = False) -> Path:
+    deps = [SYNTH_SRC, HERE / "synth_errors.cpp", SYNTH_SRC.parent / "internal.h",
+            HERE.parent / "include" / "als_gb300.h"]
+    if SYNTH_OUT.exists() and all(p.stat().st_mtime <= SYNTH_OUT.stat().st_mtime for p in deps):
+        return SYNTH_OUT
+    SYNTH_OUT.parent.mkdir(exist_ok=True)
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda_inc = Path(nvcc).resolve().parent.parent / "include"  # cuda_runtime.h (declarations)
+    tmp = SYNTH_OUT.with_suffix(".so.tmp")
+    cmd = [cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", f"-I{cuda_inc}",
+           str(SYNTH_SRC), str(HERE / "synth_errors.cpp"), "-o", str(tmp)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"generator build failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, SYNTH_OUT)
+    return SYNTH_OUT
+
+
+# The reference tree these recipes compile from: $CUDA_ALS_REFERENCE, by default the read-only
+# checkout this build was made against.  Absent on machines that only run the prebuilt files.
+REF_SRC = Path(os.environ.get("CUDA_ALS_REFERENCE", "/root/reference"))
+
 # The reference's own logger (logger.cpp, a few hundred lines of standard C++), compiled from
 # its sources where they lie, with a call-script driver: the pin of the event-log format.  Only
 # where the reference tree is present; the output stays in oracle/_ref/ (git-ignored).
-REF_SRC = Path("/root/reference")
 REF_OUT = HERE / "_ref" / f"ref_logger-{platform.machine()}"
 
 
@@ -102,5 +134,6 @@ def build_ref_cubins(verbose: bool = False) -> dict[str, Path]:
 
 if __name__ == "__main__":
     print(build(verbose=True))
+    print(build_synth(verbose=True))
     print(build_ref(verbose=True))
     print(build_ref_cubins(verbose=True))

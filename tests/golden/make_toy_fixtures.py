@@ -11,11 +11,17 @@ It also re-derives the same arrays from the shipped ratings.dat with the scripts
 (sklearn train_test_split(random_state=42), coo_matrix(...).tocsr().tocoo(), tocsr(), tocsc())
 and asserts both agree, which pins the fixture to the reference's procedure as well as its log.
 
-Run in a container that has the reference checked out:
+The re-derivation also stores the raw training and test triples of the split (0-based, in the
+order train_test_split returns them, before any scipy conversion): the input of the GPU
+triples -> CSR / CSC builder, whose output must equal the logged arrays.
+
+Run in a container that has the reference checked out (the path as the first argument, or in
+$CUDA_ALS_REFERENCE):
     python tests/golden/make_toy_fixtures.py /path/to/reference
 """
 from __future__ import annotations
 
+import os
 import re
 import sys
 from pathlib import Path
@@ -59,7 +65,10 @@ def rederive(ratings: Path, m: int, n: int, test_size: int) -> dict[str, np.ndar
     te = coo_matrix((r_te, (ui_te[:, 0] - 1, ui_te[:, 1] - 1))).tocsr().tocoo()
     tr = coo_matrix((r_tr, (ui_tr[:, 0] - 1, ui_tr[:, 1] - 1)), shape=(m, n)).tocsr().tocoo()
     csr, csc = tr.tocsr(), tr.tocsc()
-    return {"R_test_coo.data": te.data, "R_test_coo.row": te.row, "R_test_coo.col": te.col,
+    raw = {"raw_train_row": ui_tr[:, 0] - 1, "raw_train_col": ui_tr[:, 1] - 1,
+           "raw_train_val": r_tr, "raw_test_row": ui_te[:, 0] - 1,
+           "raw_test_col": ui_te[:, 1] - 1, "raw_test_val": r_te}
+    return {**raw, "R_test_coo.data": te.data, "R_test_coo.row": te.row, "R_test_coo.col": te.col,
             "R_train_csr.data": csr.data, "R_train_csr.indptr": csr.indptr,
             "R_train_csr.indices": csr.indices, "R_train_csc.data": csc.data,
             "R_train_csc.indptr": csc.indptr, "R_train_csc.indices": csc.indices}
@@ -68,17 +77,18 @@ def rederive(ratings: Path, m: int, n: int, test_size: int) -> dict[str, np.ndar
 def main(ref: Path) -> None:
     for name, (log, ratings, m, n, test_size) in TOYS.items():
         arrs = parse_log((ref / log).read_text())
-        try:
-            again = rederive(ref / ratings, m, n, test_size)
-            for k in KEYS:
-                assert np.array_equal(arrs[k], np.asarray(again[k], np.int64)), (name, k)
-            print(f"{name}: log arrays == re-derived arrays")
-        except ImportError as e:  # sklearn/scipy absent: the log alone is the fixture
-            print(f"{name}: re-derivation skipped ({e})")
+        again = rederive(ref / ratings, m, n, test_size)  # needs sklearn and scipy
+        for k in KEYS:
+            assert np.array_equal(arrs[k], np.asarray(again[k], np.int64)), (name, k)
+        print(f"{name}: log arrays == re-derived arrays")
+        raw = {k: np.asarray(v, np.int64) for k, v in again.items() if k.startswith("raw_")}
         np.savez(HERE / f"{name}.npz", m=m, n=n,
-                 **{k.replace(".", "_"): v for k, v in arrs.items()})
+                 **{k.replace(".", "_"): v for k, v in arrs.items()}, **raw)
         print(f"wrote {HERE / (name + '.npz')}")
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    where = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CUDA_ALS_REFERENCE")
+    if not where:
+        sys.exit("usage: make_toy_fixtures.py REFERENCE_TREE (or set CUDA_ALS_REFERENCE)")
+    main(Path(where))

@@ -6,6 +6,7 @@ import json
 import os
 import subprocess
 import sys
+import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -15,7 +16,10 @@ CMD = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--config"
 
 def _run(env_extra=None):
     env = dict(os.environ, **(env_extra or {}))
-    return subprocess.run(CMD, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+    t0 = time.perf_counter()
+    r = subprocess.run(CMD, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+    r.wall_s = time.perf_counter() - t0
+    return r
 
 
 def test_reference_arm_prints_one_contract_line():
@@ -36,6 +40,23 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # whole epochs, really run: the steps' claimed time fits inside the process's own wall time
+    assert d["steps"] * d["ms_per_step"] / 1e3 <= r.wall_s
+    assert "whole epochs" in cb["sample"]
+
+
+def test_reference_arm_does_not_load_the_product_library():
+    """The CPU reference arm generates its workload with the oracle-side build of the generator:
+    the product's libals_gb300.so is never mapped into its process."""
+    probe = ("import runpy, sys; sys.argv = %r; "
+             "runpy.run_path(%r, run_name='__main__'); "
+             "maps = open('/proc/self/maps').read(); "
+             "assert 'libals_gb300' not in maps, 'product library loaded'; print('CLEAN')"
+             % (["bench.py"] + CMD[2:], str(ROOT / "bench.py")))
+    r = subprocess.run([sys.executable, "-c", probe], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "CLEAN" in r.stdout
 
 
 def test_reference_arm_runs_on_rank_zero_only():
