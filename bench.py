@@ -62,7 +62,7 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", type=int, default=3, help="workload 1..5 (default 3)")
     p.add_argument("--scale", type=float, default=1.0)
-    p.add_argument("--precision", choices=["bf16", "fp32"], default=None)
+    p.add_argument("--precision", choices=["bf16", "fp8", "fp32"], default=None)
     p.add_argument("--solve", choices=["lu", "cg", "cg16", "cholesky", "auto"], default="auto",
                    help="solver of the measured sweep (default: per-bucket autotuned; cg16 = "
                         "the FP16-Gram CG, its products on the tensor core)")
@@ -395,7 +395,8 @@ def run_ours(args):
              "cg16": ca.SOLVE_TYPE.CUMF_ALS_CG_FP16,
              "cholesky": ca.SOLVE_TYPE.CHOLESKY, "auto": ca.SOLVE_TYPE.AUTO}[args.solve]
     prec_name = args.precision or ("bf16" if f <= 128 else "fp32")
-    prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16}[prec_name]
+    prec = {"fp32": ca.PRECISION.FP32, "bf16": ca.PRECISION.BF16,
+            "fp8": ca.PRECISION.FP8}[prec_name]
     stream = torch.cuda.Stream()
 
     def make(precision, how=None):
@@ -496,7 +497,7 @@ def run_ours(args):
                      "fp64_refined_rows": int(cc["fp64_refined_rows"]),
                      "flagged_rows": int(cc["flagged_rows"])}
 
-    fp32 = chol = None
+    fp32 = chol = fp8 = None
     if not args.no_compare and prec != ca.PRECISION.FP32:
         fms, fp32 = compare(ca.PRECISION.FP32, ca.SOLVE_TYPE.CHOLESKY)
         fp32.update(solve="cholesky", speedup=round(fms / ms, 3),
@@ -506,6 +507,15 @@ def run_ours(args):
             chol.update(refine_steps=1, speedup_vs_fp32=round(fms / cms, 3),
                         rmse_delta_vs_fp32=abs(chol["test_rmse_after_iters"] -
                                                fp32["test_rmse_after_iters"]))
+        # the other reduced precision of the tensor-core sweep, same solver choice
+        other = ca.PRECISION.FP8 if prec == ca.PRECISION.BF16 else ca.PRECISION.BF16
+        oms, fp8 = compare(other, solve)
+        fp8.update(precision="fp8" if other == ca.PRECISION.FP8 else "bf16",
+                   speedup_vs_fp32=round(fms / oms, 3),
+                   rmse_delta_vs_fp32=abs(fp8["test_rmse_after_iters"] -
+                                          fp32["test_rmse_after_iters"]),
+                   note="e4m3 operands with one power-of-two scale per feature, ratings in e4m3"
+                        if other == ca.PRECISION.FP8 else "BF16 operands")
 
     # ---- e2e: the same training run through the C ABI with host buffers
     e2e = None
@@ -584,7 +594,8 @@ def run_ours(args):
         "stage_ms": {k: round(v, 3) for k, v in stage.items()},
         "test_rmse_after_iters": rmse, "iters": iters, "rmse_reproduced": deterministic,
         "cold_run": cold,
-        "fp32_plain": fp32, "bf16_cholesky_refined": chol, "roofline": roofline,
+        "fp32_plain": fp32, "bf16_cholesky_refined": chol,
+        ("fp8_e4m3" if prec != ca.PRECISION.FP8 else "bf16"): fp8, "roofline": roofline,
         "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clocks, "gpu_launches": launches_per_epoch * iters * args.steps,
         "rows": rows, "flagged_rows": int(counters["flagged_rows"]),

@@ -509,6 +509,21 @@ class als_model:
                                                  C.byref(dlam)))
         return loss.value, G, dlam.value
 
+    def user_halfsweep_adjoint_f64(self, rows, cols, vals, Y, lambda_: float):
+        """The same in FP64 on the GPU from FP64 item factors Y (n x f) and lambda:
+        (loss, dL/dY as float64 n x f, dL/dlambda)."""
+        rows = np.ascontiguousarray(rows, np.int32)
+        cols = np.ascontiguousarray(cols, np.int32)
+        vals = np.ascontiguousarray(vals, np.float32)
+        Y = np.ascontiguousarray(Y, np.float64)
+        view = CsrView(self.m, self.n, len(vals), _ptr(rows), _ptr(cols), _ptr(vals))
+        loss, dlam = C.c_double(), C.c_double()
+        G = np.zeros((self.n, self.f), np.float64)
+        self._c(lib().als_user_halfsweep_adjoint_f64(self._h, C.byref(view), _ptr(Y),
+                                                     float(lambda_), C.byref(loss), _ptr(G),
+                                                     C.byref(dlam)))
+        return loss.value, G, dlam.value
+
 
 # ------------------------------------------------------------------------------------------------
 # standalone index kernels and the synthetic workloads

@@ -86,6 +86,8 @@ def lib() -> C.CDLL:
         "als_get_tuning": ([H, i32, P, P, P, P, P, C.POINTER(i32)], i32),
         "als_user_halfsweep_adjoint": ([H, C.POINTER(CooView), C.POINTER(f64), P,
                                         C.POINTER(f64)], i32),
+        "als_user_halfsweep_adjoint_f64": ([H, C.POINTER(CooView), P, f64, C.POINTER(f64), P,
+                                            C.POINTER(f64)], i32),
         "als_csr_to_csc": ([C.POINTER(CsrView), P, P, P], i32),
         "als_csr_to_csc_device": ([C.POINTER(CsrView), P, P, P, P], i32),
         "als_csr_to_csc_device_noalloc": ([C.POINTER(CsrView), P, P, P, P], i32),
@@ -127,7 +129,7 @@ EXPORTS = [
     "als_iterate", "als_half_sweep", "als_train", "als_rmse_test", "als_rmse_train",
     "als_get_factors", "als_set_factors", "als_get_device_factors", "als_save_libmf",
     "als_get_shape", "als_get_stage_ms", "als_get_counters", "als_get_plan", "als_get_tuning", "als_set_wait_limit_ns",
-    "als_user_halfsweep_adjoint", "als_csr_to_csc", "als_csr_to_csc_device",
+    "als_user_halfsweep_adjoint", "als_user_halfsweep_adjoint_f64", "als_csr_to_csc", "als_csr_to_csc_device",
     "als_csr_to_csc_device_noalloc", "als_coo_to_csr", "als_coo_to_csr_device",
     "als_degree_order", "als_partition_rows", "als_synth_shape", "als_synth_generate",
     "als_log_create", "als_log_destroy", "als_log_text", "als_log_event_started",

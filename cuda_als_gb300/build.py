@@ -26,12 +26,17 @@ SOURCES = [
     "synth.cpp",
     "index_kernels.cu",
     "coo_build.cu",
+    "init.cu",
     "sweep_fp32.cu",
     "sweep_tc.cu",
     "sweep_tc_fp32.cu",
     "sweep_tc_fp64.cu",
     "sweep_tc_fp112.cu",
     "sweep_tc_fp128.cu",
+    "sweep_tc_fp32_e4m3.cu",
+    "sweep_tc_fp64_e4m3.cu",
+    "sweep_tc_fp112_e4m3.cu",
+    "sweep_tc_fp128_e4m3.cu",
     "rmse.cu",
     "adjoint.cu",
 ]

@@ -4,12 +4,17 @@
 // als_model::train, als_model.cu:1797-2029).  Loss on held-out ratings H:
 //   L = sum_{(u,i,r) in H} (r - x_u . y_i)^2,  dL/dx_u = h_u = -2 sum_{(u,i) in H} (r - x_u.y_i) y_i.
 // Reverse: g_u = A_u^-1 h_u, solved with the same L D L^T factor as the forward solve; then
-//   dL/dy_i += r_ui g_u - (y_i . x_u) g_u - (g_u . y_i) x_u     for every training rating (u, i)
-//   dL/dy_i += -2 (r - x_u . y_i) x_u                          for every held-out rating (u, i)
-//   dL/dlambda = -sum_u n_u g_u . x_u                          (FP64, fixed-order reduction)
-// One CTA per user row: the FP32 Gram of [Y | r] in registers (as in sweep_fp32.cu), the factor
-// in shared memory, the held-out terms, the second solve, and an atomic scatter of the row's
-// contributions into dL/dY (FP32).  The held-out loss itself is summed in FP64 per CTA.
+//   dL/dy_i = sum_{u in train(i)} [(r_ui - y_i . x_u) g_u - (g_u . y_i) x_u]
+//           + sum_{u in H(i)} -2 (r_ui - x_u . y_i) x_u
+//   dL/dlambda = -sum_u n_u g_u . x_u
+// Two kernels, each in FP32 or FP64 (T):
+//   adjoint_row_kernel: one CTA per user row — the Gram of [Y | r] in register tiles (as in
+//     sweep_fp32.cu, the right-hand side summed apart with compensation), the L D L^T factor in
+//     shared memory, the forward solve, the row's held-out terms (in order: h_u and the loss),
+//     the second solve with the same factor; writes x_u and g_u, the loss and dL/dlambda parts.
+//   adjoint_item_kernel: one CTA per item — dL/dy_i from the item's training column (the CSC)
+//     and its held-out ratings, each warp a fixed subset in order, the warps combined in order:
+//     deterministic, no atomics.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -26,7 +31,10 @@ namespace als {
 namespace {
 
 constexpr int KC = 32;
-constexpr int MAX_FP = 232;
+constexpr int MAX_FP = 232;      // FP32: the Gram of FP x (FP+1) floats in shared memory
+constexpr int MAX_F_F64 = 128;   // FP64: the Gram of 136 x 137 doubles (149 KB)
+constexpr int ITEM_WARPS = 8;
+constexpr int ITEM_Q = (MAX_FP + 31) / 32;  // feature slots per lane in the item kernel
 
 __host__ __device__ inline int fp_of(int f) { return ((f + 1 + 7) / 8) * 8; }
 __host__ __device__ inline int nt_of(int fp) {
@@ -39,22 +47,24 @@ __host__ __device__ inline size_t zsize_of(int fp) {
     size_t z = (size_t)KC * fp, g = (size_t)fp * (fp + 1);
     return z > g ? z : g;
 }
+template <typename T>
 inline size_t smem_of(int fp) {
-    return sizeof(float) * (zsize_of(fp) + 2 * KC + 5 * (size_t)fp + 64);
+    return sizeof(T) * (zsize_of(fp) + 2 * KC + 5 * (size_t)fp + 64);
 }
 
+template <typename T>
 struct AdjArgs {
     const int32_t *ptr, *idx;  // training CSR of the user side
     const float *val;
     const int32_t *hptr, *hidx;  // held-out ratings grouped by user (CSR)
     const float *hval;
-    const float *Y;   // item factors (FP32, row-contiguous)
-    float *X;         // user factors out
-    float *dY;        // n x f, accumulated atomically (zeroed by the caller)
-    double *loss_part, *dlam_part;  // one per CTA
+    const T *Y;        // item factors, row-contiguous
+    T *X, *G;          // per user: x_u and g_u (m x f)
+    float *Xout;       // the handle's U (FP32 copy of x_u)
+    double *loss_part, *dlam_part;  // one per row
     int32_t *flags;
     int f;
-    float lambda;
+    T lambda;
 };
 
 __device__ double block_sum_d(double v, double *sh) {
@@ -70,36 +80,52 @@ __device__ double block_sum_d(double v, double *sh) {
     return s;  // valid in thread 0
 }
 
-__global__ void __launch_bounds__(1024) adjoint_user_kernel(const AdjArgs a, const int FP) {
-    extern __shared__ __align__(16) float smem[];
+template <typename T>
+__device__ __forceinline__ T fma_t(T a, T b, T c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024)
+    adjoint_row_kernel(const AdjArgs<T> a, const int FP) {
+    extern __shared__ __align__(16) unsigned char smem_bytes[];
+    T *smem = reinterpret_cast<T *>(smem_bytes);
     __shared__ double dsh[33];
     const int f = a.f, NB = FP / 8, GS = FP + 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int nt = blockDim.x;
-    float *Z = smem;
+    T *Z = smem;
     int32_t *scol = (int32_t *)(smem + zsize_of(FP));
-    float *sval = (float *)(scol + KC);
-    float *vb = sval + KC, *vx = vb + FP, *vh = vx + FP, *vt = vh + FP, *vq = vt + FP;
-    float *red = vq + FP;
+    T *sval = reinterpret_cast<T *>(scol) + KC;
+    T *vb = sval + KC, *vx = vb + FP, *vh = vx + FP, *red = vh + 2 * FP;
 
     const int row = blockIdx.x;
     const int beg = a.ptr[row], end = a.ptr[row + 1], nu = end - beg;
     const int hbeg = a.hptr[row], hend = a.hptr[row + 1];
-    float *xo = a.X + (int64_t)row * f;
+    T *xr = a.X + (int64_t)row * f;
+    T *gr = a.G + (int64_t)row * f;
+    float *xo = a.Xout + (int64_t)row * f;
     double loss = 0.0, dlam = 0.0;
 
-    if (nu == 0) {  // x = 0; held-out residuals are r itself, no gradient through x
-        for (int i = tid; i < f; i += nt) xo[i] = 0.f;
+    auto no_gradient = [&]() {  // x = 0: held-out residuals are r itself, no path through x
+        for (int i = tid; i < f; i += nt) {
+            xo[i] = 0.f;
+            xr[i] = T(0);
+            gr[i] = T(0);
+        }
         for (int e = hbeg + tid; e < hend; e += nt) loss += (double)a.hval[e] * a.hval[e];
         const double s = block_sum_d(loss, dsh);
         if (tid == 0) {
-            a.loss_part[blockIdx.x] = s;
-            a.dlam_part[blockIdx.x] = 0.0;
+            a.loss_part[row] = s;
+            a.dlam_part[row] = 0.0;
         }
+    };
+    if (nu == 0) {
+        no_gradient();
         return;
     }
 
-    // ---- forward: Gram of [Y | r] (lower block triangle, 4 x 8 register tiles)
+    // ---- forward: Gram of Y_u (lower block triangle, 4 x 8 register tiles), b apart
     const bool active = tid < NB * (NB + 1);
     const int q = tid >> 1;
     int bi = (int)((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
@@ -107,140 +133,176 @@ __global__ void __launch_bounds__(1024) adjoint_user_kernel(const AdjArgs a, con
     while (bi * (bi + 1) / 2 > q) --bi;
     const int bj = q - bi * (bi + 1) / 2;
     const int r0 = 8 * bi + 4 * (tid & 1), c0 = 8 * bj;
-    float acc[4][8];
+    T acc[4][8];
 #pragma unroll
     for (int p = 0; p < 4; ++p)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[p][c] = 0.f;
+        for (int c = 0; c < 8; ++c) acc[p][c] = T(0);
+    T bsum = T(0), bcomp = T(0);  // b_tid: compensated sum of 32-rating chunk sums
     for (int base = beg; base < end; base += KC) {
         const int cnt = min(KC, end - base);
         if (tid < KC) {
             scol[tid] = tid < cnt ? a.idx[base + tid] : -1;
-            sval[tid] = tid < cnt ? a.val[base + tid] : 0.f;
+            sval[tid] = tid < cnt ? (T)a.val[base + tid] : T(0);
         }
         __syncthreads();
         for (int k = warp; k < KC; k += nwarps) {
             const int c = scol[k];
-            const float rv = sval[k];
-            const float *y = a.Y + (int64_t)(c < 0 ? 0 : c) * f;
-            for (int j = lane; j < FP; j += 32) {
-                float v = 0.f;
-                if (c >= 0) v = j < f ? __ldg(y + j) : (j == f ? rv : 0.f);
-                Z[k * FP + j] = v;
-            }
+            const T *y = a.Y + (int64_t)(c < 0 ? 0 : c) * f;
+            for (int j = lane; j < FP; j += 32) Z[k * FP + j] = (c >= 0 && j < f) ? y[j] : T(0);
         }
         __syncthreads();
         if (active) {
             for (int k = 0; k < cnt; ++k) {
-                const float4 av = *reinterpret_cast<const float4 *>(&Z[k * FP + r0]);
-                const float4 cv0 = *reinterpret_cast<const float4 *>(&Z[k * FP + c0]);
-                const float4 cv1 = *reinterpret_cast<const float4 *>(&Z[k * FP + c0 + 4]);
-                const float ar[4] = {av.x, av.y, av.z, av.w};
-                const float cr[8] = {cv0.x, cv0.y, cv0.z, cv0.w, cv1.x, cv1.y, cv1.z, cv1.w};
+                const T *zk = Z + k * FP;
 #pragma unroll
                 for (int p = 0; p < 4; ++p)
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) acc[p][c] = fmaf(ar[p], cr[c], acc[p][c]);
+                    for (int c = 0; c < 8; ++c)
+                        acc[p][c] = fma_t<T>(zk[r0 + p], zk[c0 + c], acc[p][c]);
             }
+        }
+        if (tid < f) {
+            T cs = T(0);
+            for (int k = 0; k < cnt; ++k) cs = fma_t<T>(sval[k], Z[k * FP + tid], cs);
+            const T yk = cs - bcomp;
+            const T t = bsum + yk;
+            bcomp = (t - bsum) - yk;
+            bsum = t;
         }
         __syncthreads();
     }
-    float *G = Z;
+    T *Gm = Z;
     if (active) {
 #pragma unroll
         for (int p = 0; p < 4; ++p)
 #pragma unroll
-            for (int c = 0; c < 8; ++c) G[(r0 + p) * GS + c0 + c] = acc[p][c];
+            for (int c = 0; c < 8; ++c) Gm[(r0 + p) * GS + c0 + c] = acc[p][c];
     }
     __syncthreads();
-    const float reg = (float)nu * a.lambda;
-    for (int i = tid; i < f; i += nt) {
-        G[i * GS + i] += reg;
-        vb[i] = G[f * GS + i];
+    const T reg = (T)nu * a.lambda;
+    if (tid < f) {  // (the launch has at least f threads)
+        Gm[tid * GS + tid] += reg;
+        vb[tid] = bsum;
     }
     __syncthreads();
-    bool ok = ldlt_factor<CtaSync>(G, GS, f, tid, nt);
-    if (ok) ldlt_solve<CtaSync>(G, GS, f, vb, tid);  // vb <- x
+    bool ok = ldlt_factor<CtaSync>(Gm, GS, f, tid, nt);
+    if (ok) ldlt_solve<CtaSync>(Gm, GS, f, vb, tid);  // vb <- x
     __syncthreads();
-    float badf = 0.f;
-    for (int i = tid; i < f; i += nt) badf += (ok && isfinite(vb[i])) ? 0.f : 1.f;
-    badf = group_sum<CtaSync>(badf, red, tid, nt);
-    if (badf > 0.f) {  // non-positive pivot: x = 0, flagged, no gradient through this row
-        for (int i = tid; i < f; i += nt) {
-            xo[i] = 0.f;
-            vx[i] = 0.f;
-        }
+    T badf = T(0);
+    for (int i = tid; i < f; i += nt) badf += (ok && isfinite(vb[i])) ? T(0) : T(1);
+    badf = group_sum<CtaSync, T>(badf, red, tid, nt);
+    if (badf > T(0)) {  // non-positive pivot: x = 0, flagged, no gradient through this row
         if (tid == 0) atomicAdd(&a.flags[0], 1);
-        for (int e = hbeg + tid; e < hend; e += nt) loss += (double)a.hval[e] * a.hval[e];
-        const double s = block_sum_d(loss, dsh);
-        if (tid == 0) {
-            a.loss_part[blockIdx.x] = s;
-            a.dlam_part[blockIdx.x] = 0.0;
-        }
+        no_gradient();
         return;
     }
     for (int i = tid; i < f; i += nt) {
         vx[i] = vb[i];
-        xo[i] = vb[i];
-        vh[i] = 0.f;
+        xr[i] = vb[i];
+        xo[i] = (float)vb[i];
+        vh[i] = T(0);
     }
     __syncthreads();
 
-    // ---- held-out terms: loss, h = dL/dx, and the direct dL/dy_i = -2 res x_u.  The row's
-    // held-out ratings are few; warp 0 walks them in order, so h and the loss are deterministic.
+    // ---- held-out terms: loss and h = dL/dx.  The row's held-out ratings are few; warp 0 walks
+    // them in order, so h and the loss are deterministic.
     if (warp == 0) {
         for (int e = hbeg; e < hend; ++e) {
-            const int c = a.hidx[e];
-            const float *y = a.Y + (int64_t)c * f;
-            float d = 0.f;
-            for (int j = lane; j < f; j += 32) d = fmaf(vx[j], __ldg(y + j), d);
+            const T *y = a.Y + (int64_t)a.hidx[e] * f;
+            T d = T(0);
+            for (int j = lane; j < f; j += 32) d = fma_t<T>(vx[j], y[j], d);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-            const float res = a.hval[e] - d;
-            if (lane == 0) loss += (double)res * res;
-            float *gy = a.dY + (int64_t)c * f;
-            for (int j = lane; j < f; j += 32) {
-                vh[j] += -2.f * res * __ldg(y + j);
-                atomicAdd(&gy[j], -2.f * res * vx[j]);
-            }
+            const T res = (T)a.hval[e] - d;
+            if (lane == 0) loss += (double)res * (double)res;
+            for (int j = lane; j < f; j += 32) vh[j] += T(-2) * res * y[j];
             __syncwarp();
         }
     }
     __syncthreads();
 
     // ---- g = A^-1 h with the same factor (vh <- g)
-    ldlt_solve<CtaSync>(G, GS, f, vh, tid);
+    ldlt_solve<CtaSync>(Gm, GS, f, vh, tid);
     {
-        float gx = 0.f;
+        T gx = T(0);
         for (int i = tid; i < f; i += nt) gx += vh[i] * vx[i];
-        gx = group_sum<CtaSync>(gx, red, tid, nt);
+        gx = group_sum<CtaSync, T>(gx, red, tid, nt);
         dlam = -(double)nu * (double)gx;
     }
-
-    // ---- dL/dy_i += r g - (y.x) g - (g.y) x over the row's training ratings
-    for (int e = beg + warp; e < end; e += nwarps) {
-        const int c = a.idx[e];
-        const float r = a.val[e];
-        const float *y = a.Y + (int64_t)c * f;
-        float yx = 0.f, gy = 0.f;
-        for (int j = lane; j < f; j += 32) {
-            const float yj = __ldg(y + j);
-            yx = fmaf(yj, vx[j], yx);
-            gy = fmaf(yj, vh[j], gy);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            yx += __shfl_xor_sync(0xffffffffu, yx, o);
-            gy += __shfl_xor_sync(0xffffffffu, gy, o);
-        }
-        float *out = a.dY + (int64_t)c * f;
-        for (int j = lane; j < f; j += 32)
-            atomicAdd(&out[j], (r - yx) * vh[j] - gy * vx[j]);
-    }
+    for (int i = tid; i < f; i += nt) gr[i] = vh[i];
     const double sl = block_sum_d(loss, dsh);
     if (tid == 0) {
-        a.loss_part[blockIdx.x] = sl;
-        a.dlam_part[blockIdx.x] = dlam;
+        a.loss_part[row] = sl;
+        a.dlam_part[row] = dlam;
+    }
+}
+
+// dL/dy_i of item i: its training column (CSC: users and ratings) and its held-out ratings.
+// Warp w takes entries w, w + ITEM_WARPS, ... in order; lane l holds features l, l + 32, ...;
+// the warps' partial vectors are added in warp order.
+template <typename T>
+__global__ void __launch_bounds__(32 * ITEM_WARPS)
+    adjoint_item_kernel(int64_t n, int f, const int32_t *__restrict__ cptr,
+                        const int32_t *__restrict__ cusr, const float *__restrict__ cval,
+                        const int32_t *__restrict__ hptr, const int32_t *__restrict__ husr,
+                        const float *__restrict__ hval, const T *__restrict__ Y,
+                        const T *__restrict__ X, const T *__restrict__ G, T *__restrict__ dY) {
+    extern __shared__ __align__(16) unsigned char smem_bytes[];
+    T *part = reinterpret_cast<T *>(smem_bytes);  // [ITEM_WARPS][f]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nq = (f + 31) / 32;
+    for (int64_t it = blockIdx.x; it < n; it += gridDim.x) {
+        T y[ITEM_Q], acc[ITEM_Q];
+#pragma unroll
+        for (int q = 0; q < ITEM_Q; ++q) {
+            const int j = lane + 32 * q;
+            y[q] = q < nq && j < f ? Y[it * f + j] : T(0);
+            acc[q] = T(0);
+        }
+        auto dot = [&](const T *v) -> T {
+            T s = T(0);
+#pragma unroll
+            for (int q = 0; q < ITEM_Q; ++q) {
+                const int j = lane + 32 * q;
+                if (q < nq && j < f) s = fma_t<T>(y[q], v[j], s);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            return s;
+        };
+        for (int e = cptr[it] + warp; e < cptr[it + 1]; e += ITEM_WARPS) {
+            const T *xu = X + (int64_t)cusr[e] * f;
+            const T *gu = G + (int64_t)cusr[e] * f;
+            const T yx = dot(xu), gy = dot(gu);
+            const T c = (T)cval[e] - yx;
+#pragma unroll
+            for (int q = 0; q < ITEM_Q; ++q) {
+                const int j = lane + 32 * q;
+                if (q < nq && j < f) acc[q] = fma_t<T>(c, gu[j], fma_t<T>(-gy, xu[j], acc[q]));
+            }
+        }
+        for (int e = hptr[it] + warp; e < hptr[it + 1]; e += ITEM_WARPS) {
+            const T *xu = X + (int64_t)husr[e] * f;
+            const T res = (T)hval[e] - dot(xu);
+#pragma unroll
+            for (int q = 0; q < ITEM_Q; ++q) {
+                const int j = lane + 32 * q;
+                if (q < nq && j < f) acc[q] = fma_t<T>(T(-2) * res, xu[j], acc[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < ITEM_Q; ++q) {
+            const int j = lane + 32 * q;
+            if (q < nq && j < f) part[warp * f + j] = acc[q];
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < f; j += blockDim.x) {
+            T s = part[j];
+            for (int w = 1; w < ITEM_WARPS; ++w) s += part[w * f + j];
+            dY[it * f + j] = s;
+        }
+        __syncthreads();
     }
 }
 
@@ -252,88 +314,113 @@ __global__ void sum_doubles_kernel(const double *__restrict__ v, int64_t n, doub
     if (threadIdx.x == 0) *out = s;
 }
 
-}  // namespace
-}  // namespace als
+__global__ void f64_to_f32_kernel(const double *__restrict__ a, int64_t n, float *__restrict__ b) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
 
-using namespace als;
+// Counting sort of the held-out triples by `key` (rows or columns), stable: ptr (nkeys + 1),
+// the other index and the value per entry.
+void group_by(int64_t nkeys, int64_t nh, const int32_t *key, const int32_t *other,
+              const float *vals, std::vector<int32_t> &ptr, std::vector<int32_t> &oth,
+              std::vector<float> &val) {
+    ptr.assign((size_t)nkeys + 1, 0);
+    oth.assign((size_t)(nh > 0 ? nh : 1), 0);
+    val.assign((size_t)(nh > 0 ? nh : 1), 0.f);
+    for (int64_t e = 0; e < nh; ++e) ptr[key[e] + 1]++;
+    for (int64_t r = 0; r < nkeys; ++r) ptr[r + 1] += ptr[r];
+    std::vector<int32_t> cur(ptr.begin(), ptr.end() - 1);
+    for (int64_t e = 0; e < nh; ++e) {
+        const int32_t p = cur[key[e]]++;
+        oth[p] = other[e];
+        val[p] = vals[e];
+    }
+}
 
-als_status run_adjoint(als_handle *h, const als_coo_view *held, double *loss, float *dLdY,
-                       double *dLdlambda) {
-    if (held->rows != h->m || held->cols != h->n || held->nnz < 0 || held->nnz > INT32_MAX ||
-        (held->nnz > 0 && (!held->row_idxs || !held->col_idxs || !held->vals)))
-        return set_global_error(ALS_ERR_INVALID_ARG, "held-out COO shape differs from the model");
+// The adjoint in precision T.  Y: device item factors in T (n x f); dLdY: host, n x f of
+// OutT (float for the FP32 entry point, double for the FP64 one).
+template <typename T, typename OutT>
+als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T lambda,
+                        double *loss, OutT *dLdY, double *dLdlambda) {
     const int f = h->f;
     const int FP = fp_of(f);
-    if (FP > MAX_FP) return set_global_error(ALS_ERR_UNSUPPORTED, "adjoint supports f <= 231");
-    cudaSetDevice(h->cfg.device);
-    // group the held-out ratings by user on the host (counting sort, stable)
     const int64_t m = h->m, n = h->n, nh = held->nnz;
-    std::vector<int32_t> hptr((size_t)m + 1, 0), hidx((size_t)(nh > 0 ? nh : 1));
-    std::vector<float> hval((size_t)(nh > 0 ? nh : 1));
-    for (int64_t e = 0; e < nh; ++e) {
-        const int32_t r = held->row_idxs[e], c = held->col_idxs[e];
-        if (r < 0 || r >= m || c < 0 || c >= n || !std::isfinite(held->vals[e]))
-            return set_global_error(ALS_ERR_INVALID_ARG, "held-out entry out of range at " +
-                                                             std::to_string(e));
-        hptr[r + 1]++;
-    }
-    for (int64_t r = 0; r < m; ++r) hptr[r + 1] += hptr[r];
-    {
-        std::vector<int32_t> cur(hptr.begin(), hptr.end() - 1);
-        for (int64_t e = 0; e < nh; ++e) {
-            const int32_t p = cur[held->row_idxs[e]]++;
-            hidx[p] = held->col_idxs[e];
-            hval[p] = held->vals[e];
-        }
-    }
+    std::vector<int32_t> hptr_u, hcol_u, hptr_i, hrow_i;
+    std::vector<float> hval_u, hval_i;
+    group_by(m, nh, held->row_idxs, held->col_idxs, held->vals, hptr_u, hcol_u, hval_u);
+    group_by(n, nh, held->col_idxs, held->row_idxs, held->vals, hptr_i, hrow_i, hval_i);
     cudaStream_t st = h->stream;
-    int32_t *d_hptr = nullptr, *d_hidx = nullptr;
-    float *d_hval = nullptr, *d_dY = nullptr;
+    int32_t *d_hptr_u = nullptr, *d_hcol_u = nullptr, *d_hptr_i = nullptr, *d_hrow_i = nullptr;
+    float *d_hval_u = nullptr, *d_hval_i = nullptr;
+    T *d_X = nullptr, *d_G = nullptr, *d_dY = nullptr;
     double *d_parts = nullptr;
     cudaError_t e = cudaSuccess;
     auto step = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    step(cudaMalloc(&d_hptr, sizeof(int32_t) * (m + 1)));
-    step(cudaMalloc(&d_hidx, sizeof(int32_t) * hidx.size()));
-    step(cudaMalloc(&d_hval, sizeof(float) * hval.size()));
-    step(cudaMalloc(&d_dY, sizeof(float) * (size_t)(n * f)));
+    const size_t nhp = hcol_u.size();
+    step(cudaMalloc(&d_hptr_u, sizeof(int32_t) * (m + 1)));
+    step(cudaMalloc(&d_hcol_u, sizeof(int32_t) * nhp));
+    step(cudaMalloc(&d_hval_u, sizeof(float) * nhp));
+    step(cudaMalloc(&d_hptr_i, sizeof(int32_t) * (n + 1)));
+    step(cudaMalloc(&d_hrow_i, sizeof(int32_t) * nhp));
+    step(cudaMalloc(&d_hval_i, sizeof(float) * nhp));
+    step(cudaMalloc(&d_X, sizeof(T) * (size_t)(m * f)));
+    step(cudaMalloc(&d_G, sizeof(T) * (size_t)(m * f)));
+    step(cudaMalloc(&d_dY, sizeof(T) * (size_t)(n * f)));
     step(cudaMalloc(&d_parts, sizeof(double) * (size_t)(2 * m + 2)));
     if (e == cudaSuccess) {
-        step(cudaMemcpyAsync(d_hptr, hptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
-        step(cudaMemcpyAsync(d_hidx, hidx.data(), sizeof(int32_t) * hidx.size(), cudaMemcpyHostToDevice, st));
-        step(cudaMemcpyAsync(d_hval, hval.data(), sizeof(float) * hval.size(), cudaMemcpyHostToDevice, st));
-        step(cudaMemsetAsync(d_dY, 0, sizeof(float) * (size_t)(n * f), st));
+        step(cudaMemcpyAsync(d_hptr_u, hptr_u.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_hcol_u, hcol_u.data(), sizeof(int32_t) * nhp, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_hval_u, hval_u.data(), sizeof(float) * nhp, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_hptr_i, hptr_i.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_hrow_i, hrow_i.data(), sizeof(int32_t) * nhp, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_hval_i, hval_i.data(), sizeof(float) * nhp, cudaMemcpyHostToDevice, st));
         step(cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, st));
-        AdjArgs a{};
+        AdjArgs<T> a{};
         a.ptr = h->d_csr_ptr;
         a.idx = h->d_csr_idx;
         a.val = h->d_csr_val;
-        a.hptr = d_hptr;
-        a.hidx = d_hidx;
-        a.hval = d_hval;
-        a.Y = h->d_V;
-        a.X = h->d_U;
-        a.dY = d_dY;
+        a.hptr = d_hptr_u;
+        a.hidx = d_hcol_u;
+        a.hval = d_hval_u;
+        a.Y = d_Y;
+        a.X = d_X;
+        a.G = d_G;
+        a.Xout = h->d_U;
         a.loss_part = d_parts;
         a.dlam_part = d_parts + m;
         a.flags = h->d_flags;
         a.f = f;
-        a.lambda = h->cfg.lambda;
-        const size_t smem = smem_of(FP);
+        a.lambda = lambda;
+        const size_t smem = smem_of<T>(FP);
         if (smem > 48 * 1024)
-            step(cudaFuncSetAttribute(adjoint_user_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-        if (e == cudaSuccess) adjoint_user_kernel<<<(unsigned)m, nt_of(FP), smem, st>>>(a, FP);
+            step(cudaFuncSetAttribute(adjoint_row_kernel<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (e == cudaSuccess && m > 0) adjoint_row_kernel<T><<<(unsigned)m, nt_of(FP), smem, st>>>(a, FP);
+        step(cudaGetLastError());
+        const size_t ismem = sizeof(T) * ITEM_WARPS * (size_t)f;
+        if (e == cudaSuccess && n > 0)
+            adjoint_item_kernel<T><<<(unsigned)std::min<int64_t>(n, 152 * 16), 32 * ITEM_WARPS,
+                                     ismem, st>>>(n, f, h->d_csc_ptr, h->d_csc_idx, h->d_csc_val,
+                                                  d_hptr_i, d_hrow_i, d_hval_i, d_Y, d_X, d_G,
+                                                  d_dY);
         step(cudaGetLastError());
         sum_doubles_kernel<<<1, 256, 0, st>>>(d_parts, m, d_parts + 2 * m);
         sum_doubles_kernel<<<1, 256, 0, st>>>(d_parts + m, m, d_parts + 2 * m + 1);
         double out[2] = {0.0, 0.0};
         step(cudaMemcpyAsync(out, d_parts + 2 * m, sizeof(out), cudaMemcpyDeviceToHost, st));
-        if (dLdY) step(cudaMemcpyAsync(dLdY, d_dY, sizeof(float) * (size_t)(n * f), cudaMemcpyDeviceToHost, st));
+        if (dLdY) {
+            if (sizeof(OutT) == sizeof(T)) {
+                step(cudaMemcpyAsync(dLdY, d_dY, sizeof(T) * (size_t)(n * f), cudaMemcpyDeviceToHost, st));
+            } else {  // (T = double with float output does not occur)
+                step(cudaErrorInvalidValue);
+            }
+        }
         step(cudaStreamSynchronize(st));
         if (loss) *loss = out[0];
         if (dLdlambda) *dLdlambda = out[1];
     }
-    void *all[] = {d_hptr, d_hidx, d_hval, d_dY, d_parts};
+    void *all[] = {d_hptr_u, d_hcol_u, d_hval_u, d_hptr_i, d_hrow_i, d_hval_i, d_X, d_G, d_dY, d_parts};
     for (void *p : all)
         if (p) cudaFree(p);
     if (e != cudaSuccess) {
@@ -341,5 +428,64 @@ als_status run_adjoint(als_handle *h, const als_coo_view *held, double *loss, fl
         return set_global_error(e == cudaErrorMemoryAllocation ? ALS_ERR_OUT_OF_MEMORY : ALS_ERR_CUDA,
                                 h->last_error);
     }
+    int32_t flags[4] = {0, 0, 0, 0};
+    if (cudaMemcpy(flags, h->d_flags, sizeof(flags), cudaMemcpyDeviceToHost) == cudaSuccess)
+        h->counters[1] = flags[0];
     return ALS_OK;
+}
+
+als_status check_heldout(const als_handle *h, const als_coo_view *held) {
+    if (held->rows != h->m || held->cols != h->n || held->nnz < 0 || held->nnz > INT32_MAX ||
+        (held->nnz > 0 && (!held->row_idxs || !held->col_idxs || !held->vals)))
+        return set_global_error(ALS_ERR_INVALID_ARG, "held-out COO shape differs from the model");
+    for (int64_t e = 0; e < held->nnz; ++e) {
+        const int32_t r = held->row_idxs[e], c = held->col_idxs[e];
+        if (r < 0 || r >= h->m || c < 0 || c >= h->n || !std::isfinite(held->vals[e]))
+            return set_global_error(ALS_ERR_INVALID_ARG, "held-out entry out of range at " +
+                                                             std::to_string(e));
+    }
+    return ALS_OK;
+}
+
+}  // namespace
+}  // namespace als
+
+using namespace als;
+
+als_status run_adjoint(als_handle *h, const als_coo_view *held, double *loss, float *dLdY,
+                       double *dLdlambda) {
+    als_status s = check_heldout(h, held);
+    if (s != ALS_OK) return s;
+    if (fp_of(h->f) > MAX_FP) return set_global_error(ALS_ERR_UNSUPPORTED, "adjoint supports f <= 231");
+    cudaSetDevice(h->cfg.device);
+    return adjoint_impl<float, float>(h, held, h->d_V, h->cfg.lambda, loss, dLdY, dLdlambda);
+}
+
+als_status run_adjoint_f64(als_handle *h, const als_coo_view *held, const double *Y,
+                           double lambda, double *loss, double *dLdY, double *dLdlambda) {
+    als_status s = check_heldout(h, held);
+    if (s != ALS_OK) return s;
+    if (!Y) return set_global_error(ALS_ERR_INVALID_ARG, "null item factors");
+    if (h->f > MAX_F_F64)
+        return set_global_error(ALS_ERR_UNSUPPORTED, "the FP64 adjoint supports f <= 128");
+    if (!(lambda >= 0.0) || !std::isfinite(lambda))
+        return set_global_error(ALS_ERR_INVALID_ARG, "lambda must be finite and >= 0");
+    cudaSetDevice(h->cfg.device);
+    const size_t nf = (size_t)h->n * h->f;
+    double *d_Y = nullptr;
+    cudaError_t e = cudaMalloc(&d_Y, sizeof(double) * (nf ? nf : 1));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_Y, Y, sizeof(double) * nf, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && nf) {  // the handle's V follows, rounded to FP32
+        f64_to_f32_kernel<<<(unsigned)std::min<size_t>((nf + 255) / 256, 152 * 16), 256, 0,
+                            h->stream>>>(d_Y, (int64_t)nf, h->d_V);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        if (d_Y) cudaFree(d_Y);
+        return set_global_error(ALS_ERR_CUDA, std::string("adjoint: ") + cudaGetErrorString(e));
+    }
+    s = adjoint_impl<double, double>(h, held, d_Y, lambda, loss, dLdY, dLdlambda);
+    cudaFree(d_Y);
+    return s;
 }

@@ -308,14 +308,6 @@ static als_status validate_config(const als_config &c, std::string *why) {
         *why = "precision must be fp32, bf16 or fp8";
         return ALS_ERR_INVALID_ARG;
     }
-    if (p == ALS_PREC_FP8) {
-        // A per-row e4m3 scale of the gathered factors varies along the contraction (ratings), so
-        // it cannot be taken out of Y_u^T Y_u, and 8-bit tcgen05 operands want the K-major
-        // (ratings-contiguous) panel the gather does not produce; the BF16 path is the
-        // reduced-precision sweep of this library.
-        *why = "precision fp8 (e4m3 Gram) is not built; use bf16";
-        return ALS_ERR_UNSUPPORTED;
-    }
     if (p == ALS_PREC_FP32 && !fp32_supported(c.f)) {
         *why = "f too large for the FP32 path (max 231)";
         return ALS_ERR_UNSUPPORTED;
@@ -586,16 +578,9 @@ extern "C" als_status als_init_factors(als_handle *h) {
     if (!h) return set_global_error(ALS_ERR_INVALID_ARG, "null handle");
     cudaSetDevice(h->cfg.device);
     if (h->cfg.autotune) reset_tuning(h);  // a new run re-tunes the ALS_SOLVE_AUTO plan
-    // als_model.cu:1772-1777: srand(0), VT[k] = 0.2*((float)rand()/(float)RAND_MAX), UT = 0
-    std::srand(0u);
-    const int64_t nf = h->n * h->f;
-    for (int64_t k = 0; k < nf; ++k)
-        h->h_V[k] = (float)(0.2 * (double)((float)std::rand() / (float)RAND_MAX));
-    std::fill(h->h_U.begin(), h->h_U.end(), 0.f);
-    H_CUDA(h, cudaMemcpyAsync(h->d_V, h->h_V.data(), sizeof(float) * nf, cudaMemcpyHostToDevice,
-                              h->stream));
-    H_CUDA(h, cudaMemsetAsync(h->d_U, 0, sizeof(float) * h->m * h->f, h->stream));
-    H_CUDA(h, cudaStreamSynchronize(h->stream));
+    // als_model.cu:1772-1777: srand(0), VT[k] = 0.2*((float)rand()/(float)RAND_MAX), UT = 0,
+    // generated on the GPU bit for bit (init.cu: glibc's rand() sequence by jump-ahead)
+    H_CUDA(h, init_factors_device(h->m, h->n, h->f, h->d_U, h->d_V, h->stream));
     return ALS_OK;
 }
 

@@ -65,6 +65,12 @@ size_t degree_order_scratch_bytes(int64_t rows);
 cudaError_t degree_order_device(int64_t rows, const int32_t *ptr, int32_t max_degree,
                                 int32_t *perm, void *scratch, cudaStream_t st);
 
+// The reference's srand(0) factor initialisation (als_model.cu:1772-1784) on the device: V gets
+// 0.2 * rand() / RAND_MAX for its n f entries in order (glibc's sequence, bit for bit), U zeros.
+// Synchronous on `st`.
+cudaError_t init_factors_device(int64_t m, int64_t n, int f, float *U, float *V,
+                                cudaStream_t st);
+
 // Expand CSR row pointers into one row index per entry.
 cudaError_t expand_rows(int64_t rows, int64_t nnz, const int32_t *ptr, int32_t *coo_rows,
                         cudaStream_t st);

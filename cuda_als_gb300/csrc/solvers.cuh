@@ -23,21 +23,21 @@ struct NamedSync {
     __device__ static void sync() { asm volatile("bar.sync %0, %1;" ::"n"(ID), "n"(NT) : "memory"); }
 };
 
-// Deterministic group sum (fixed combination order); red holds >= 33 floats.
-template <class Sync>
-__device__ float group_sum(float v, float *red, int tid, int nt) {
+// Deterministic group sum (fixed combination order); red holds >= 33 values.
+template <class Sync, typename T = float>
+__device__ T group_sum(T v, T *red, int tid, int nt) {
     const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp] = v;
     Sync::sync();
     if (tid == 0) {
-        float s = 0.f;
+        T s = T(0);
         for (int w = 0; w < nwarps; ++w) s += red[w];
         red[32] = s;
     }
     Sync::sync();
-    const float s = red[32];
+    const T s = red[32];
     Sync::sync();
     return s;
 }
@@ -64,15 +64,15 @@ __device__ void sym_matvec(const float *G, int gs, int f, const float *p, float 
 // Square-root-free Cholesky A = L D L^T in place on the lower triangle (right-looking; the
 // multipliers l_ik = a_ik / d_k are applied on the fly, one barrier per column).  Returns false,
 // uniformly over the group, on a pivot that is not positive and finite.
-template <class Sync>
-__device__ bool ldlt_factor(float *G, int gs, int f, int tid, int nt) {
+template <class Sync, typename T>
+__device__ bool ldlt_factor(T *G, int gs, int f, int tid, int nt) {
     const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     for (int k = 0; k < f; ++k) {
-        const float piv = G[k * gs + k];
-        if (!(piv > 0.f) || !isfinite(piv)) return false;
-        const float inv = 1.0f / piv;
+        const T piv = G[k * gs + k];
+        if (!(piv > T(0)) || !isfinite(piv)) return false;
+        const T inv = T(1) / piv;
         for (int i = k + 1 + warp; i < f; i += nwarps) {
-            const float lik = G[i * gs + k] * inv;
+            const T lik = G[i * gs + k] * inv;
             for (int j = k + 1 + lane; j <= i; j += 32) G[i * gs + j] -= lik * G[j * gs + k];
         }
         Sync::sync();
@@ -81,20 +81,20 @@ __device__ bool ldlt_factor(float *G, int gs, int f, int tid, int nt) {
 }
 
 // b <- (L D L^T)^-1 b, by the group's first warp.
-template <class Sync>
-__device__ void ldlt_solve(const float *G, int gs, int f, float *b, int tid) {
+template <class Sync, typename T>
+__device__ void ldlt_solve(const T *G, int gs, int f, T *b, int tid) {
     if ((tid >> 5) == 0) {
         const int lane = tid & 31;
         for (int k = 0; k < f; ++k) {  // L z = b
-            const float zk = b[k];
-            const float inv = 1.0f / G[k * gs + k];
+            const T zk = b[k];
+            const T inv = T(1) / G[k * gs + k];
             for (int i = k + 1 + lane; i < f; i += 32) b[i] -= G[i * gs + k] * inv * zk;
             __syncwarp();
         }
         for (int k = lane; k < f; k += 32) b[k] = b[k] / G[k * gs + k];  // D w = z
         __syncwarp();
         for (int k = f - 1; k >= 0; --k) {  // L^T x = w
-            const float xk = b[k];
+            const T xk = b[k];
             for (int i = lane; i < k; i += 32) b[i] -= G[k * gs + i] / G[i * gs + i] * xk;
             __syncwarp();
         }

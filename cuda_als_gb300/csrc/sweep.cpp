@@ -426,3 +426,10 @@ extern "C" als_status als_user_halfsweep_adjoint(als_handle *h, const als_coo_vi
     if (!h || !heldout) return set_global_error(ALS_ERR_INVALID_ARG, "null argument");
     return run_adjoint(h, heldout, loss, dLdY, dLdlambda);
 }
+
+extern "C" als_status als_user_halfsweep_adjoint_f64(als_handle *h, const als_coo_view *heldout,
+                                                     const double *Y, double lambda, double *loss,
+                                                     double *dLdY, double *dLdlambda) {
+    if (!h || !heldout) return set_global_error(ALS_ERR_INVALID_ARG, "null argument");
+    return run_adjoint_f64(h, heldout, Y, lambda, loss, dLdY, dLdlambda);
+}

@@ -34,6 +34,7 @@
 // drains its own MMAs and copies, frees TMEM and returns; the host reports ALS_ERR_TIMEOUT.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -61,6 +62,67 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
     }
 }
 
+// FP8 (e4m3) copy of a factor table with one power-of-two scale per feature: d_j = 2^e_j with
+// the smallest e_j that puts the column's largest magnitude at or below 448 (e4m3's largest
+// finite value), so max |Y_.j| / d_j lies in (224, 448] and no value saturates; then
+// q_rj = e4m3(Y_rj / d_j) (round to nearest even), rows of 128 bytes (features f..127 zero).
+// Because d is a power of two, Y_u^T Y_u = D (Q_u^T Q_u) D and Y_u^T r = D Q_u^T r exactly: one
+// scale per row and column of every Gram, applied when the solver reads the accumulator.
+__global__ void colmax_kernel(const float *__restrict__ Y, int64_t rows, int f,
+                              unsigned int *__restrict__ cmax) {
+    __shared__ unsigned int sm[MAXF];
+    for (int j = threadIdx.x; j < MAXF; j += blockDim.x) sm[j] = 0u;
+    __syncthreads();
+    const int64_t total = rows * (int64_t)f;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e % f);
+        const float a = fabsf(Y[e]);
+        // non-negative floats order as their bit patterns; NaN (above +inf) surfaces as a NaN
+        // scale, whose rows the solver flags as non-finite
+        atomicMax(&sm[j], __float_as_uint(a));
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < f; j += blockDim.x)
+        if (sm[j]) atomicMax(&cmax[j], sm[j]);
+}
+
+// The scale exponent of a column from the bit pattern of its largest magnitude.
+__device__ __forceinline__ int e4m3_scale_exp(unsigned int bits) {
+    if (bits == 0u) return 0;
+    const int E = (int)((bits >> 23) & 0xffu) - 127;  // (subnormal maxima: E = -127)
+    const unsigned int mant = bits & 0x7fffffu;
+    // max = m 2^E, m in [1, 2): max / 2^(E-8) = 256 m <= 448 iff m <= 1.75
+    const int e = mant <= 0x600000u ? E - 8 : E - 7;
+    return e < -126 ? -126 : (e > 127 ? 127 : e);
+}
+
+__global__ void quantise_e4m3_kernel(const float *__restrict__ Y, int64_t rows, int f,
+                                     const unsigned int *__restrict__ cmax,
+                                     float *__restrict__ dscale, uint8_t *__restrict__ out) {
+    __shared__ float inv[MAXF];
+    for (int j = threadIdx.x; j < MAXF; j += blockDim.x) {
+        const int e = j < f ? e4m3_scale_exp(cmax[j]) : 0;
+        inv[j] = __uint_as_float((uint32_t)(127 - e) << 23);  // 2^-e (|e| <= 126: normal)
+        if (blockIdx.x == 0) dscale[j] = __uint_as_float((uint32_t)(127 + e) << 23);
+    }
+    __syncthreads();
+    const int64_t total = rows * (int64_t)(F8_ROW_BYTES / 4);  // four bytes per thread step
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = w / (F8_ROW_BYTES / 4);
+        const int j0 = (int)(w - r * (F8_ROW_BYTES / 4)) * 4;
+        uint32_t word = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = j0 + k;
+            const float v = j < f ? Y[r * f + j] * inv[j] : 0.f;
+            word |= (uint32_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3) << (8 * k);
+        }
+        reinterpret_cast<uint32_t *>(out)[w] = word;
+    }
+}
+
 }  // namespace tcg
 }  // namespace als
 
@@ -77,9 +139,13 @@ static int tcg_solver(int solve_type) {
     }
 }
 struct TcState {
-    CUtensorMap tmap[2];   // [side]: TMA map of d_bf[side] (64-byte aligned member first)
+    CUtensorMap tmap[2];   // [side]: TMA map of the side's 16- or 8-bit table (64-byte aligned)
     tcg::Geometry geo[tcg::NSOLVER];  // per solver (CG, Cholesky, LU, tensor-core CG)
+    bool f8 = false;                   // FP8 (e4m3) operands instead of BF16
     __nv_bfloat16 *d_bf[2] = {nullptr, nullptr};  // [side]: table gathered by that side
+    uint8_t *d_f8[2] = {nullptr, nullptr};        // [side]: FP8 table (rows of 128 bytes)
+    float *d_scale[2] = {nullptr, nullptr};       // [side]: its per-feature scales [MAXF]
+    unsigned int *d_cmax = nullptr;               // column maxima (bit patterns) [MAXF]
     int32_t *d_work = nullptr;                     // one row counter per bucket
     int num_sms = 0;
     cudaEvent_t ev_q[2] = {nullptr, nullptr};
@@ -119,6 +185,20 @@ static bool encode_table_map(CUtensorMap *map, void *table, int64_t rows, int fs
               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The gather map of an FP8 table of `rows` x 128 bytes: box = 128 features (one 128-byte line,
+// the swizzle span) x 1 row.
+static bool encode_table_map_f8(CUtensorMap *map, void *table, int64_t rows) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)tcg::F8_ROW_BYTES, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)tcg::F8_ROW_BYTES};
+    const cuuint32_t box[2] = {(cuuint32_t)tcg::F8_ROW_BYTES, 1};
+    const cuuint32_t estride[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, table, dims, strides, box, estride,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 als_status tc_prepare(als_handle *h, std::string *why) {
     if (!tc_path_supported(h->f)) {
         *why = "tensor-core path supports f in 1..128";
@@ -136,14 +216,32 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     }
     TcState *t = new TcState();
     h->tc = t;
+    t->f8 = h->precision == ALS_PREC_FP8;
     size_t smem_max = 0;
     for (int sv = 0; sv < tcg::NSOLVER; ++sv) {
-        t->geo[sv] = tcg::geometry(h->f, sv);
+        t->geo[sv] = tcg::geometry(h->f, sv, t->f8);
         smem_max = std::max(smem_max, t->geo[sv].smem);
     }
     t->num_sms = sms;
     const int64_t opp[2] = {h->n, h->m};  // side 0 gathers V rows, side 1 gathers U rows
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < 2 && t->f8; ++s) {
+        const size_t bytes = (size_t)tcg::F8_ROW_BYTES * (size_t)(opp[s] + 1);
+        if (cudaMalloc(&t->d_f8[s], bytes) != cudaSuccess ||
+            cudaMemset(t->d_f8[s], 0, bytes) != cudaSuccess ||
+            cudaMalloc(&t->d_scale[s], sizeof(float) * tcg::MAXF) != cudaSuccess) {
+            *why = "out of memory for the FP8 factor tables";
+            return ALS_ERR_OUT_OF_MEMORY;
+        }
+        if (!encode_table_map_f8(&t->tmap[s], t->d_f8[s], opp[s] + 1)) {
+            *why = "cuTensorMapEncodeTiled failed for the FP8 table";
+            return ALS_ERR_CUDA;
+        }
+    }
+    if (t->f8 && cudaMalloc(&t->d_cmax, sizeof(unsigned int) * tcg::MAXF) != cudaSuccess) {
+        *why = "out of memory";
+        return ALS_ERR_OUT_OF_MEMORY;
+    }
+    for (int s = 0; s < 2 && !t->f8; ++s) {
         const size_t bytes = sizeof(__nv_bfloat16) * (size_t)(opp[s] + 1) * t->geo[0].fst;
         if (cudaMalloc(&t->d_bf[s], bytes) != cudaSuccess ||
             cudaMemset(t->d_bf[s], 0, bytes) != cudaSuccess) {
@@ -164,10 +262,10 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     // inside a timed region (the autotuner's) loads a module
     cudaError_t e;
     switch (t->geo[0].fp) {
-    case 32: e = tcg::configure_32(smem_max); break;
-    case 64: e = tcg::configure_64(smem_max); break;
-    case 112: e = tcg::configure_112(smem_max); break;
-    default: e = tcg::configure_128(smem_max); break;
+    case 32: e = t->f8 ? tcg::configure_32_e4m3(smem_max) : tcg::configure_32(smem_max); break;
+    case 64: e = t->f8 ? tcg::configure_64_e4m3(smem_max) : tcg::configure_64(smem_max); break;
+    case 112: e = t->f8 ? tcg::configure_112_e4m3(smem_max) : tcg::configure_112(smem_max); break;
+    default: e = t->f8 ? tcg::configure_128_e4m3(smem_max) : tcg::configure_128(smem_max); break;
     }
     if (e != cudaSuccess) {
         *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
@@ -181,6 +279,11 @@ void tc_release(als_handle *h) {
     if (!t) return;
     for (auto p : t->d_bf)
         if (p) cudaFree(p);
+    for (auto p : t->d_f8)
+        if (p) cudaFree(p);
+    for (auto p : t->d_scale)
+        if (p) cudaFree(p);
+    if (t->d_cmax) cudaFree(t->d_cmax);
     if (t->d_work) cudaFree(t->d_work);
     for (auto e : t->ev_q)
         if (e) cudaEventDestroy(e);
@@ -199,6 +302,24 @@ als_status tc_quantise(als_handle *h, int side, int *launches, std::string *why)
     const int64_t opp = side == 0 ? h->n : h->m;
     const float *Y = side == 0 ? h->d_V : h->d_U;
     record_event(t->ev_q[0], h->stream);
+    if (t->f8) {
+        const int grid = (int)std::max<int64_t>(
+            1, std::min<int64_t>((opp * h->f + 255) / 256, (int64_t)t->num_sms * 8));
+        cudaError_t e = cudaMemsetAsync(t->d_cmax, 0, sizeof(unsigned int) * tcg::MAXF, h->stream);
+        if (e == cudaSuccess) {
+            tcg::colmax_kernel<<<grid, 256, 0, h->stream>>>(Y, opp, h->f, t->d_cmax);
+            tcg::quantise_e4m3_kernel<<<grid, 256, 0, h->stream>>>(Y, opp, h->f, t->d_cmax,
+                                                                   t->d_scale[side], t->d_f8[side]);
+            *launches += 2;
+            e = cudaGetLastError();
+        }
+        record_event(t->ev_q[1], h->stream);
+        if (e != cudaSuccess) {
+            *why = std::string("FP8 quantise: ") + cudaGetErrorString(e);
+            return ALS_ERR_CUDA;
+        }
+        return ALS_OK;
+    }
     const int64_t total = opp * t->geo[0].fst;
     const int grid = (int)std::max<int64_t>(
         1, std::min<int64_t>((total + 255) / 256, (int64_t)t->num_sms * 8));
@@ -232,6 +353,7 @@ cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t 
     p.val = side == 0 ? h->d_csr_val : h->d_csc_val;
     p.order = h->d_order[side] + lo;
     p.Ybf = t->d_bf[side];
+    p.dscale = t->d_scale[side];
     p.X = side == 0 ? h->d_U : h->d_V;
     p.work = t->d_work + slot;
     p.flags = h->d_flags;
@@ -254,10 +376,14 @@ cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t 
     const int grid = (int)std::min<int64_t>(p.nrows, t->num_sms);
     if (grid <= 0) return cudaSuccess;
     switch (g.fp) {
-    case 32: tcg::launch_32(p, g, grid, st); break;
-    case 64: tcg::launch_64(p, g, grid, st); break;
-    case 112: tcg::launch_112(p, g, grid, st); break;
-    default: tcg::launch_128(p, g, grid, st); break;
+    case 32: t->f8 ? tcg::launch_32_e4m3(p, g, grid, st) : tcg::launch_32(p, g, grid, st); break;
+    case 64: t->f8 ? tcg::launch_64_e4m3(p, g, grid, st) : tcg::launch_64(p, g, grid, st); break;
+    case 112:
+        t->f8 ? tcg::launch_112_e4m3(p, g, grid, st) : tcg::launch_112(p, g, grid, st);
+        break;
+    default:
+        t->f8 ? tcg::launch_128_e4m3(p, g, grid, st) : tcg::launch_128(p, g, grid, st);
+        break;
     }
     ++*launches;
     return cudaGetLastError();

@@ -4,9 +4,9 @@
 
 namespace als {
 namespace tcg {
-cudaError_t configure_112(size_t smem) { return configure_fp<112>(smem); }
+cudaError_t configure_112(size_t smem) { return configure_fp<112, false>(smem); }
 void launch_112(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
-    launch_fp<112>(p, g, grid, st);
+    launch_fp<112, false>(p, g, grid, st);
 }
 }  // namespace tcg
 }  // namespace als

@@ -4,9 +4,9 @@
 
 namespace als {
 namespace tcg {
-cudaError_t configure_128(size_t smem) { return configure_fp<128>(smem); }
+cudaError_t configure_128(size_t smem) { return configure_fp<128, false>(smem); }
 void launch_128(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
-    launch_fp<128>(p, g, grid, st);
+    launch_fp<128, false>(p, g, grid, st);
 }
 }  // namespace tcg
 }  // namespace als

@@ -4,9 +4,9 @@
 
 namespace als {
 namespace tcg {
-cudaError_t configure_32(size_t smem) { return configure_fp<32>(smem); }
+cudaError_t configure_32(size_t smem) { return configure_fp<32, false>(smem); }
 void launch_32(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
-    launch_fp<32>(p, g, grid, st);
+    launch_fp<32, false>(p, g, grid, st);
 }
 }  // namespace tcg
 }  // namespace als

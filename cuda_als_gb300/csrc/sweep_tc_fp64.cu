@@ -4,9 +4,9 @@
 
 namespace als {
 namespace tcg {
-cudaError_t configure_64(size_t smem) { return configure_fp<64>(smem); }
+cudaError_t configure_64(size_t smem) { return configure_fp<64, false>(smem); }
 void launch_64(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
-    launch_fp<64>(p, g, grid, st);
+    launch_fp<64, false>(p, g, grid, st);
 }
 }  // namespace tcg
 }  // namespace als

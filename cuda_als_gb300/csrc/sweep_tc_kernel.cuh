@@ -5,6 +5,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -98,6 +99,7 @@ struct Params {
     const int32_t *ptr, *idx, *order;
     const float *val;
     const __nv_bfloat16 *Ybf;  // (n_opp + 1) x fst, row n_opp all zero
+    const float *dscale;       // FP8 operands: the table's per-feature scales (powers of two)
     float *X;                  // this side's FP32 factors (in: CG warm start, out: solution)
     int32_t *work;             // atomic row counter (zeroed before the launch)
     int32_t *flags;            // [0] flagged rows, [1] FP64-refined rows, [2] timeouts
@@ -134,6 +136,12 @@ struct Geometry {
     int fp, fst, ng, acc_stride, tmem_cols, nbuf, nepi, nthreads;
     size_t smem;
 };
+// FP8 (e4m3) operands: each gathered factor row is one 128-byte line (features 0..127, one byte
+// each: the table's row pitch), so a stage's panel is one 128-feature swizzle atom of KC
+// ratings, and one MMA covers K = 32 ratings.  The per-feature scales of the table sit in shared
+// memory behind the solver groups' scratch.
+constexpr int F8_ROW_BYTES = 128;
+constexpr int F8_K = 32;
 
 __host__ __device__ inline int gs_of(int f) { return (f + 1) % 2 ? f + 1 : f + 2; }
 
@@ -151,7 +159,7 @@ constexpr size_t group_floats(int fp, int solver) {
                          : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
 }
 
-inline Geometry geometry(int f, int solver) {
+inline Geometry geometry(int f, int solver, bool f8 = false) {
     Geometry g;
     g.fp = fp_of(f);
     g.fst = (f + 7) / 8 * 8;
@@ -167,6 +175,7 @@ inline Geometry geometry(int f, int solver) {
     const int ns = nstage_of(solver, g.fp);
     size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
+    if (f8) bytes += sizeof(float) * MAXF;                            // per-feature scales
     bytes += MRING_BYTES;                                            // metadata ring
     bytes += 1024;                                                   // metas, barriers, scalars
     g.smem = bytes + 1024;                                           // 1024-B alignment slack
@@ -227,9 +236,13 @@ __device__ __forceinline__ bool mbar_wait_warp(uint32_t bar, uint32_t parity, vo
 __device__ __forceinline__ void fence_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-// 4-byte asynchronous global -> shared copy (the ratings of a stage have no alignment).
-__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+// 4-byte asynchronous global -> shared copy (the ratings of a stage have no alignment), with an
+// L2 cache policy: the column ids and ratings stream through once per half-sweep (evict first),
+// so they do not push the gathered factor table (evict last) out of L2.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, uint64_t policy) {
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;" ::"r"(dst),
+                 "l"(src), "l"(policy)
+                 : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
@@ -254,6 +267,11 @@ __device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap *tma
         "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(bar),
         "l"(policy)
         : "memory");
+}
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
 }
 __device__ __forceinline__ uint64_t l2_evict_last_policy() {
     uint64_t pol;
@@ -289,6 +307,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// Instruction descriptor of tcgen05.mma kind::f8f6f4: D F32, A/B E4M3 (format 0), majors, N, M.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N, bool a_mn, bool b_mn) {
+    return (1u << 4) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_e4m3(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
@@ -549,10 +580,14 @@ __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, 
 // The solver warpgroup's work on one row whose Gram row i sits in TMEM at tb.
 // Returns true when it released the accumulator itself (arrived on `release` once every thread
 // of the group had read its row out of TMEM); otherwise the caller releases it afterwards.
-template <int FP, int SOLVER>
+// With FP8 operands (F8) the accumulator holds Q^T Q and Q^T r of the scaled table Q = Y D^-1
+// (D = diag(dsc), powers of two): every value read from TMEM is multiplied back, A_ij by
+// d_i d_j and b_i by d_i, which is exact.
+template <int FP, int SOLVER, bool F8>
 __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, int et, int g,
                           float *gsm, const GroupSync &gs, uint32_t release, float xw,
-                          uint32_t mvbar, CgTcState &cst, volatile int *abort, bool &ok) {
+                          uint32_t mvbar, CgTcState &cst, volatile int *abort, bool &ok,
+                          const float *dsc) {
     float *Ls = gsm;
     float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
@@ -561,12 +596,13 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     const int f = p.f;
     float *xo = p.X + (int64_t)m.row * f;
     const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
+    const float di = F8 && i < FP ? dsc[i] : 1.f;  // this thread's row scale (1 unless FP8)
 
     float bi = 0.f;
     if constexpr (SOLVER == SOLVER_CHOL) {
         float v[16];
         tmem_ld16(tb + p.ng, v);
-        bi = i < f ? v[0] : 0.f;
+        bi = i < f ? v[0] * di : 0.f;
     }
     int slot = 0;
     float xi = 0.f;
@@ -595,6 +631,11 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 #pragma unroll
                         for (int j = 0; j < 16; ++j) v[h + j] = 0.f;
                     }
+                }
+                if constexpr (F8) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        if (c + j < FP) v[j] *= di * dsc[c + j];
                 }
 #pragma unroll
                 for (int j = 0; j < 32; ++j)  // padded rows (i >= f): the identity
@@ -635,10 +676,10 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             xi = i < f ? yv[i] : 0.f;
             const bool wide = cflag[1] != 0;
             for (int s = 0; s < p.refine_steps; ++s) {
-                if (i < FP) sv[i] = xi;
+                if (i < FP) sv[i] = xi * di;  // (FP8: sum_j A'_ij d_j x_j, then times d_i)
                 gs.sync();
-                const double ax = wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
-                                       : tmem_rowdot<FP, false>(tb, p.ng, sv);
+                const double ax = (wide ? tmem_rowdot<FP, true>(tb, p.ng, sv)
+                                        : tmem_rowdot<FP, false>(tb, p.ng, sv)) * (double)di;
                 float ri;
                 if (wide)
                     ri = (float)((double)bi - ax - (double)reg * (double)xi);
@@ -667,7 +708,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     if (lg + h + j == i) dii = v[j];
             }
         }
-        dii = i < f ? dii + reg : 0.f;
+        dii = i < f ? dii * di * di + reg : 0.f;
         const float dmax = gmax128(dii, red, slot, gs);
         const int ka = exp2_of(dmax) > 14 ? exp2_of(dmax) - 14 : 0;
         const float sa = pow2f(-ka);
@@ -676,13 +717,17 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         {
             float b0, b1;
             tmem_ld2(tb + p.ng, b0, b1);
-            bi = i < f ? b0 : 0.f;
+            bi = i < f ? b0 * di : 0.f;
         }
 #pragma unroll
         for (int c = 0; c < FP; c += 16) {
             if (c < p.ng) {  // warp-uniform
                 float v[16];
                 tmem_ld16(tb + c, v);
+                if constexpr (F8) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] *= di * dsc[c + j];
+                }
                 uint32_t w[8];
 #pragma unroll
                 for (int j = 0; j < 16; j += 2) {
@@ -715,13 +760,17 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             {
                 float b0, b1;
                 tmem_ld2(tb + p.ng, b0, b1);
-                bi = i < f ? b0 : 0.f;
+                bi = i < f ? b0 * di : 0.f;
             }
 #pragma unroll
             for (int k = 0; k < NK; ++k) {
                 float v[16];
                 if (16 * k < p.ng) {  // warp-uniform
                     tmem_ld16(tb + 16 * k, v);
+                    if constexpr (F8) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) v[j] *= di * dsc[16 * k + j];
+                    }
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[j] = 0.f;
@@ -761,8 +810,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             float b;
             tmem_ld_row(tb, (uint32_t)p.ng, a, b);
 #pragma unroll
-            for (int j = 0; j < FP; ++j) a[j] = j < p.ng && i < f ? a[j] : 0.f;
-            bi = i < f ? b : 0.f;
+            for (int j = 0; j < FP; ++j) a[j] = j < p.ng && i < f ? (F8 ? a[j] * di * dsc[j] : a[j]) : 0.f;
+            bi = i < f ? b * di : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < FP; ++j)
@@ -806,7 +855,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     return released;
 }
 
-template <int FP, int SOLVER>
+template <int FP, int SOLVER, bool F8>
 __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
     constexpr int NSTAGE = nstage_of(SOLVER, FP);
@@ -821,13 +870,14 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     // ready and issues M=128 x N=ng+16 (Gram in columns [0, ng), b in column ng; row ng of the
     // accumulator then holds b^T, a padded row the solvers ignore).  Where the gather warps have
     // the time: the tensor-core CG's six; FP = 128 (ng = 128) has no free column.
-    constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112;
+    constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112 && !F8;
     static_assert(NGATHER <= MAX_NGATHER, "");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
     float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
-    int32_t *mcol = (int32_t *)(gscratch + GroupLayout<FP, SOLVER>::floats * NEPI);    // [MR][KC]
+    float *dsc = gscratch + GroupLayout<FP, SOLVER>::floats * NEPI;  // [MAXF] FP8 scales
+    int32_t *mcol = (int32_t *)(dsc + (F8 ? MAXF : 0));                             // [MR][KC]
     float *mval = reinterpret_cast<float *>(mcol + MR * KC);                            // [MR][KC]
     Meta *mmeta = reinterpret_cast<Meta *>(mval + MR * KC);                             // [MR]
     Meta *smeta = reinterpret_cast<Meta *>(mmeta + MR);                                 // [NSTAGE]
@@ -857,6 +907,9 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     if constexpr (SOLVER == SOLVER_CGTC) {  // the groups' operand tiles: columns 2..15 stay zero
         for (int i = tid; i < (int)(GroupLayout<FP, SOLVER>::floats * NEPI / 4); i += blockDim.x)
             reinterpret_cast<float4 *>(gscratch)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if constexpr (F8) {  // padded features scale by 1 (their values are zero)
+        for (int j = tid; j < MAXF; j += blockDim.x) dsc[j] = j < p.f ? p.dscale[j] : 1.f;
     }
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) {
@@ -927,6 +980,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             n1beg = lane < n1cnt ? p.ptr[n1row] : 0;
             n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
         }
+        const uint64_t stream_pol = l2_evict_first_policy();  // column ids and ratings: once
         int aj = 0;                                          // look-ahead cursor: row of chunk
         int abase = __shfl_sync(0xffffffffu, cbeg, 0);       // and first rating of its stage
         uint32_t gen = 0;                                    // stages issued by the look-ahead
@@ -976,8 +1030,8 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
 #pragma unroll
             for (int h = 0; h < KC; h += 32) {
                 if (lane + h < cnt) {
-                    cp_async4(smem_u32(mc + lane + h), p.idx + abase + lane + h);
-                    cp_async4(smem_u32(mv + lane + h), p.val + abase + lane + h);
+                    cp_async4(smem_u32(mc + lane + h), p.idx + abase + lane + h, stream_pol);
+                    cp_async4(smem_u32(mv + lane + h), p.val + abase + lane + h, stream_pol);
                 } else {
                     mc[lane + h] = p.zero_row;   // the ragged tail gathers the all-zero row
                     mv[lane + h] = 0.f;
@@ -1037,8 +1091,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     } else if (warp == WM) {
         // ------------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc_g = idesc_bf16(128, FUSED ? p.ng + 16 : p.ng, true, true);
-            const uint32_t idesc_r = idesc_bf16(128, 16, true, false);
+            const uint32_t idesc_g = F8 ? idesc_e4m3(128, p.ng, true, true)
+                                        : idesc_bf16(128, FUSED ? p.ng + 16 : p.ng, true, true);
+            const uint32_t idesc_r = F8 ? idesc_e4m3(128, 16, true, false)
+                                        : idesc_bf16(128, 16, true, false);
             const uint32_t ring_s = smem_u32(ring);
             uint32_t it = 0, acc_it = 0, buf = 0;
             bool ok = true;
@@ -1075,16 +1131,30 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 const uint32_t dg = tmem_base + buf * p.acc_stride;
                 const uint32_t db = dg + p.ng;
                 const uint32_t tile_s = ring_s + s * STAGE_BYTES;
-                const int nk = (m.cnt + 15) >> 4;
-                for (int kk = 0; kk < nk; ++kk) {
-                    const uint64_t ad = sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
-
-                    const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
-                    mma_bf16(dg, ad, ad, idesc_g, accum);
-                    if (!FUSED) {
-                        const uint64_t rd =
-                            sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
-                        mma_bf16(db, ad, rd, idesc_r, accum);
+                if constexpr (F8) {
+                    // K = 32 ratings (four 8-rating groups, 4 KB of the one-atom panel) and the
+                    // matching 32 bytes of the rating tile's row per MMA
+                    const int nk = (m.cnt + F8_K - 1) / F8_K;
+                    for (int kk = 0; kk < nk; ++kk) {
+                        const uint64_t ad =
+                            sdesc(tile_s + kk * 4 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
+                        const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
+                        mma_e4m3(dg, ad, ad, idesc_g, accum);
+                        const uint64_t rd = sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                        mma_e4m3(db, ad, rd, idesc_r, accum);
+                    }
+                } else {
+                    const int nk = (m.cnt + 15) >> 4;
+                    for (int kk = 0; kk < nk; ++kk) {
+                        const uint64_t ad =
+                            sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
+                        const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
+                        mma_bf16(dg, ad, ad, idesc_g, accum);
+                        if (!FUSED) {
+                            const uint64_t rd =
+                                sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                            mma_bf16(db, ad, rd, idesc_r, accum);
+                        }
                     }
                 }
                 mma_commit(smem_u32(&empty[s]));
@@ -1139,9 +1209,9 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             bool released = false;
             if (m.nu > 0) {
                 const uint32_t tb = tmem_base + ((uint32_t)lanegrp << 16) + buf * p.acc_stride;
-                released = solve_row<FP, SOLVER>(p, m, tb, i, et, g, gsm, gs,
-                                                 smem_u32(&acc_empty[buf]), xw,
-                                                 smem_u32(&mvbar[g]), cst, abort, ok);
+                released = solve_row<FP, SOLVER, F8>(p, m, tb, i, et, g, gsm, gs,
+                                                     smem_u32(&acc_empty[buf]), xw,
+                                                     smem_u32(&mvbar[g]), cst, abort, ok, dsc);
             } else if (i < p.f) {
                 p.X[(int64_t)m.row * p.f + i] = 0.f;  // no ratings: defined as x = 0
             }
@@ -1168,7 +1238,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         // with the byte count and issues one tile::gather4 per lane (4 ratings x 64 features).
         // The warp whose turn comes after the last stage writes the end marker (row = -1).
         const int h = warp - WG;
-        const int natoms = p.fst > 64 ? 2 : 1;
+        const int natoms = F8 ? 1 : (p.fst > 64 ? 2 : 1);
         const int gq = lane & 15, ga = lane >> 4;  // this lane's 4-rating quad, atom
         const uint64_t keep = l2_evict_last_policy();
         bool ok = true;
@@ -1253,11 +1323,18 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             }
             uint8_t *tile = ring + s * STAGE_BYTES;
             __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
-            rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
-            rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
-            // the MMA reads ratings [0, 16 nk): gather 4 nk quads (the ragged tail's column ids
-            // point at the zero row), 512 bytes per quad and atom
-            const int nq = ((m.cnt + 15) >> 4) * 4;
+            if constexpr (F8) {  // e4m3 ratings (star ratings are exact), bytes 0..63 of row 0
+                uint8_t *rt8 = tile + TILE_BYTES;
+                rt8[lane] = __nv_cvt_float_to_fp8(mval[slot * KC + lane], __NV_SATFINITE, __NV_E4M3);
+                rt8[lane + 32] =
+                    __nv_cvt_float_to_fp8(mval[slot * KC + lane + 32], __NV_SATFINITE, __NV_E4M3);
+            } else {
+                rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
+                rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
+            }
+            // the MMA reads ratings [0, 16 nk) (FP8: [0, 32 nk)): gather their quads (the ragged
+            // tail's column ids point at the zero row), 512 bytes per quad and atom
+            const int nq = F8 ? ((m.cnt + F8_K - 1) / F8_K) * (F8_K / 4) : ((m.cnt + 15) >> 4) * 4;
             const bool mine = gq < nq && ga < natoms;
             int32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
             if (mine) {
@@ -1328,9 +1405,9 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                      : "memory");
 }
 
-// Per padded size FP (one translation unit each, compiled in parallel): set the shared-memory
-// limit of the four solver variants and launch the selected one.
-template <int FP>
+// Per padded size FP and operand type (one translation unit each, compiled in parallel): set the
+// shared-memory limit of the four solver variants and launch the selected one.
+template <int FP, bool F8>
 cudaError_t configure_fp(size_t smem) {
     // the host's geometry and the kernel's per-group layout agree
     static_assert(group_floats(FP, SOLVER_CG) == GroupLayout<FP, SOLVER_CG>::floats, "");
@@ -1343,33 +1420,37 @@ cudaError_t configure_fp(size_t smem) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if ((size_t)maxsm < smem) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CG>,
+    cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CG, F8>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CHOL>,
+        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CHOL, F8>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_LU>,
+        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_LU, F8>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CGTC>,
+        e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CGTC, F8>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     return e;
 }
 
-template <int FP>
+template <int FP, bool F8>
 void launch_fp(const Params &p, const Geometry &g, int grid, cudaStream_t st) {
     switch (p.solve) {
-    case SOLVER_CG: sweep_tc_kernel<FP, SOLVER_CG><<<grid, g.nthreads, g.smem, st>>>(p); break;
-    case SOLVER_LU: sweep_tc_kernel<FP, SOLVER_LU><<<grid, g.nthreads, g.smem, st>>>(p); break;
-    case SOLVER_CGTC: sweep_tc_kernel<FP, SOLVER_CGTC><<<grid, g.nthreads, g.smem, st>>>(p); break;
-    default: sweep_tc_kernel<FP, SOLVER_CHOL><<<grid, g.nthreads, g.smem, st>>>(p); break;
+    case SOLVER_CG: sweep_tc_kernel<FP, SOLVER_CG, F8><<<grid, g.nthreads, g.smem, st>>>(p); break;
+    case SOLVER_LU: sweep_tc_kernel<FP, SOLVER_LU, F8><<<grid, g.nthreads, g.smem, st>>>(p); break;
+    case SOLVER_CGTC:
+        sweep_tc_kernel<FP, SOLVER_CGTC, F8><<<grid, g.nthreads, g.smem, st>>>(p);
+        break;
+    default: sweep_tc_kernel<FP, SOLVER_CHOL, F8><<<grid, g.nthreads, g.smem, st>>>(p); break;
     }
 }
 
 #define ALS_TC_DECLARE(FP)                                                                 \
     cudaError_t configure_##FP(size_t smem);                                               \
-    void launch_##FP(const Params &p, const Geometry &g, int grid, cudaStream_t st);
+    void launch_##FP(const Params &p, const Geometry &g, int grid, cudaStream_t st);       \
+    cudaError_t configure_##FP##_e4m3(size_t smem);                                        \
+    void launch_##FP##_e4m3(const Params &p, const Geometry &g, int grid, cudaStream_t st);
 ALS_TC_DECLARE(32)
 ALS_TC_DECLARE(64)
 ALS_TC_DECLARE(112)

@@ -15,3 +15,5 @@ cudaError_t tc_launch_bucket(const als_handle *h, int side, int32_t lo, int32_t 
                              int slot, int *launches);
 als_status run_adjoint(als_handle *h, const als_coo_view *heldout, double *loss, float *dLdY,
                        double *dLdlambda);
+als_status run_adjoint_f64(als_handle *h, const als_coo_view *heldout, const double *Y,
+                           double lambda, double *loss, double *dLdY, double *dLdlambda);

@@ -69,7 +69,8 @@ enum {
     ALS_PREC_FROM_VTVS = -1,   /* derive from calculate_vtvs_type (0-4 -> FP32, 5-7 -> BF16)       */
     ALS_PREC_FP32 = 0,
     ALS_PREC_BF16 = 1,
-    ALS_PREC_FP8 = 2           /* e4m3 with a per-row scale: reserved, rejected with UNSUPPORTED   */
+    ALS_PREC_FP8 = 2           /* e4m3 operands, one power-of-two scale per feature (per row and
+                                  column of every Gram: exact), ratings in e4m3; f <= 128     */
 };
 
 /* Model configuration.  The first block holds the reference's INI keys and als_model ctor
@@ -265,10 +266,20 @@ als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg, float
 
 /* Held-out loss L = sum over (u,i,r) in heldout of (r - x_u . y_i)^2 where X = argmin of the
  * user half-sweep given Y = V.  Computes X (written to the handle's U), L, dL/dY (n*f floats,
- * host) and dL/dlambda by solving A_u g_u = dL/dx_u with each row's Cholesky factor.
+ * host) and dL/dlambda by solving A_u g_u = dL/dx_u with each row's L D L^T factor, in FP32.
+ * dL/dY is summed per item over its ratings in a fixed order (deterministic).
  * `heldout` is a host COO view (rows index U, cols index V). */
 als_status als_user_halfsweep_adjoint(als_handle *h, const als_coo_view *heldout, double *loss,
                                       float *dLdY, double *dLdlambda);
+
+/* The same, everything in FP64 on the GPU (Gram, factor, both solves, the reverse pass), from
+ * FP64 item factors Y (n*f doubles, host) and an FP64 lambda rather than the handle's FP32 V and
+ * lambda; dL/dY is returned in FP64 (n*f doubles, host).  The handle's V receives Y rounded to
+ * FP32 and its U the forward solution.  f <= 128.  For gradient checks against finite
+ * differences and for the hyper-gradient of lambda at full precision. */
+als_status als_user_halfsweep_adjoint_f64(als_handle *h, const als_coo_view *heldout,
+                                          const double *Y, double lambda, double *loss,
+                                          double *dLdY, double *dLdlambda);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Index kernels                                                                              */

@@ -145,15 +145,18 @@ def test_no_device_fails_loudly():
                       t["R_train_csr_data"])
 
 
-def test_fp8_precision_is_refused_before_any_device_work(toy):
-    """FP8 (e4m3) is reserved in the ABI but not built: the configuration is rejected as
-    UNSUPPORTED, never silently run at another precision."""
+def test_fp8_precision_is_validated_before_any_device_work(toy):
+    """FP8 (e4m3) runs on the tensor-core path, f in 1..128: beyond it the configuration is
+    rejected as UNSUPPORTED before any device work; within it, validation passes and (on a
+    machine without a GPU) the call stops at the missing device, never at another precision."""
     tr = ca.host_sparse_matrix(toy["m"], toy["n"], len(toy["R_train_csr_data"])).set_csr(
         toy["R_train_csr_indptr"], toy["R_train_csr_indices"], toy["R_train_csr_data"])
     with pytest.raises(ca.ALSError) as e:
-        ca.als_model(tr, None, 8, 0.05, 1, precision=int(ca.PRECISION.FP8))
+        ca.als_model(tr, None, 200, 0.05, 1, precision=int(ca.PRECISION.FP8))
     assert e.value.status == ca.Status.UNSUPPORTED
-    assert "fp8" in str(e.value)
+    with pytest.raises(ca.ALSError) as e:
+        ca.als_model(tr, None, 8, 0.05, 1, precision=int(ca.PRECISION.FP8))
+    assert e.value.status == ca.Status.NO_DEVICE
 
 
 @pytest.mark.parametrize("config,scale", [(1, 1.0), (2, 0.05), (3, 0.03), (4, 0.03), (5, 0.03)])
