@@ -492,8 +492,10 @@ def run_ours(args):
         cms = run(ref) / iters
         crmse = ref.rsme_test()
         cc = ref.counters()
+        cst = ref.stage_ms()  # (the last epoch's halves)
         ref.close()
-        return cms, {"ms_per_epoch": round(cms, 3), "test_rmse_after_iters": crmse,
+        return cms, {"ms_per_epoch": round(cms, 3), "last_epoch_U_ms": round(cst["U"], 3),
+                     "last_epoch_V_ms": round(cst["V"], 3), "test_rmse_after_iters": crmse,
                      "fp64_refined_rows": int(cc["fp64_refined_rows"]),
                      "flagged_rows": int(cc["flagged_rows"])}
 

@@ -12,12 +12,14 @@
 //     sweep_fp32.cu, the right-hand side summed apart with compensation), the L D L^T factor in
 //     shared memory, the forward solve, the row's held-out terms (in order: h_u and the loss),
 //     the second solve with the same factor; writes x_u and g_u, the loss and dL/dlambda parts.
-//   adjoint_item_kernel: one CTA per item — dL/dy_i from the item's training column (the CSC)
-//     and its held-out ratings, each warp a fixed subset in order, the warps combined in order:
-//     deterministic, no atomics.
+//   adjoint_chunk_kernel + adjoint_combine_kernel: dL/dy_i from the item's training column (the
+//     CSC) in chunks of 2,048 ratings (one CTA each: heavy items spread over many) and its
+//     held-out ratings; every sum in a fixed order (warps, then chunks): deterministic, no
+//     atomics.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -35,6 +37,7 @@ constexpr int MAX_FP = 232;      // FP32: the Gram of FP x (FP+1) floats in shar
 constexpr int MAX_F_F64 = 128;   // FP64: the Gram of 136 x 137 doubles (149 KB)
 constexpr int ITEM_WARPS = 8;
 constexpr int ITEM_Q = (MAX_FP + 31) / 32;  // feature slots per lane in the item kernel
+constexpr int32_t ITEM_CHUNK = 2048;        // training ratings per chunk of an item's column
 
 __host__ __device__ inline int fp_of(int f) { return ((f + 1 + 7) / 8) * 8; }
 __host__ __device__ inline int nt_of(int fp) {
@@ -155,11 +158,30 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024)
         if (active) {
             for (int k = 0; k < cnt; ++k) {
                 const T *zk = Z + k * FP;
+                T ar[4], cr[8];  // 16-byte loads (r0 a multiple of 4, c0 of 8)
+                if constexpr (sizeof(T) == 4) {
+                    const float4 a4 = *reinterpret_cast<const float4 *>(zk + r0);
+                    const float4 c4 = *reinterpret_cast<const float4 *>(zk + c0);
+                    const float4 d4 = *reinterpret_cast<const float4 *>(zk + c0 + 4);
+                    ar[0] = a4.x; ar[1] = a4.y; ar[2] = a4.z; ar[3] = a4.w;
+                    cr[0] = c4.x; cr[1] = c4.y; cr[2] = c4.z; cr[3] = c4.w;
+                    cr[4] = d4.x; cr[5] = d4.y; cr[6] = d4.z; cr[7] = d4.w;
+                } else {
+#pragma unroll
+                    for (int p = 0; p < 4; p += 2) {
+                        const double2 v = *reinterpret_cast<const double2 *>(zk + r0 + p);
+                        ar[p] = v.x; ar[p + 1] = v.y;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 8; c += 2) {
+                        const double2 v = *reinterpret_cast<const double2 *>(zk + c0 + c);
+                        cr[c] = v.x; cr[c + 1] = v.y;
+                    }
+                }
 #pragma unroll
                 for (int p = 0; p < 4; ++p)
 #pragma unroll
-                    for (int c = 0; c < 8; ++c)
-                        acc[p][c] = fma_t<T>(zk[r0 + p], zk[c0 + c], acc[p][c]);
+                    for (int c = 0; c < 8; ++c) acc[p][c] = fma_t<T>(ar[p], cr[c], acc[p][c]);
             }
         }
         if (tid < f) {
@@ -238,21 +260,26 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024)
     }
 }
 
-// dL/dy_i of item i: its training column (CSC: users and ratings) and its held-out ratings.
-// Warp w takes entries w, w + ITEM_WARPS, ... in order; lane l holds features l, l + 32, ...;
-// the warps' partial vectors are added in warp order.
+// dL/dy_i, in fixed chunks: chunk c covers ratings [cbeg[c], cend[c]) of item citem[c]'s
+// training column (the CSC: users and ratings) and, for the item's first chunk, its held-out
+// ratings.  Warp w of the chunk's CTA takes entries w, w + ITEM_WARPS, ... in order; lane l
+// holds features l, l + 32, ...; the warps' partial vectors are added in warp order into
+// part[c].  Heavy items (hundreds of thousands of ratings) spread over many CTAs this way.
 template <typename T>
 __global__ void __launch_bounds__(32 * ITEM_WARPS)
-    adjoint_item_kernel(int64_t n, int f, const int32_t *__restrict__ cptr,
-                        const int32_t *__restrict__ cusr, const float *__restrict__ cval,
-                        const int32_t *__restrict__ hptr, const int32_t *__restrict__ husr,
-                        const float *__restrict__ hval, const T *__restrict__ Y,
-                        const T *__restrict__ X, const T *__restrict__ G, T *__restrict__ dY) {
+    adjoint_chunk_kernel(int64_t nchunks, int f, const int32_t *__restrict__ citem,
+                         const int32_t *__restrict__ cbeg, const int32_t *__restrict__ cend,
+                         const int32_t *__restrict__ cusr, const float *__restrict__ cval,
+                         const int32_t *__restrict__ hptr, const int32_t *__restrict__ husr,
+                         const float *__restrict__ hval, const T *__restrict__ Y,
+                         const T *__restrict__ X, const T *__restrict__ G, T *__restrict__ part) {
     extern __shared__ __align__(16) unsigned char smem_bytes[];
-    T *part = reinterpret_cast<T *>(smem_bytes);  // [ITEM_WARPS][f]
+    T *wp = reinterpret_cast<T *>(smem_bytes);  // [ITEM_WARPS][f]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nq = (f + 31) / 32;
-    for (int64_t it = blockIdx.x; it < n; it += gridDim.x) {
+    for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int64_t it = citem[ch];
+        const bool first = ch == 0 || citem[ch - 1] != it;
         T y[ITEM_Q], acc[ITEM_Q];
 #pragma unroll
         for (int q = 0; q < ITEM_Q; ++q) {
@@ -271,7 +298,7 @@ __global__ void __launch_bounds__(32 * ITEM_WARPS)
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             return s;
         };
-        for (int e = cptr[it] + warp; e < cptr[it + 1]; e += ITEM_WARPS) {
+        for (int e = cbeg[ch] + warp; e < cend[ch]; e += ITEM_WARPS) {
             const T *xu = X + (int64_t)cusr[e] * f;
             const T *gu = G + (int64_t)cusr[e] * f;
             const T yx = dot(xu), gy = dot(gu);
@@ -282,27 +309,43 @@ __global__ void __launch_bounds__(32 * ITEM_WARPS)
                 if (q < nq && j < f) acc[q] = fma_t<T>(c, gu[j], fma_t<T>(-gy, xu[j], acc[q]));
             }
         }
-        for (int e = hptr[it] + warp; e < hptr[it + 1]; e += ITEM_WARPS) {
-            const T *xu = X + (int64_t)husr[e] * f;
-            const T res = (T)hval[e] - dot(xu);
+        if (first) {
+            for (int e = hptr[it] + warp; e < hptr[it + 1]; e += ITEM_WARPS) {
+                const T *xu = X + (int64_t)husr[e] * f;
+                const T res = (T)hval[e] - dot(xu);
 #pragma unroll
-            for (int q = 0; q < ITEM_Q; ++q) {
-                const int j = lane + 32 * q;
-                if (q < nq && j < f) acc[q] = fma_t<T>(T(-2) * res, xu[j], acc[q]);
+                for (int q = 0; q < ITEM_Q; ++q) {
+                    const int j = lane + 32 * q;
+                    if (q < nq && j < f) acc[q] = fma_t<T>(T(-2) * res, xu[j], acc[q]);
+                }
             }
         }
 #pragma unroll
         for (int q = 0; q < ITEM_Q; ++q) {
             const int j = lane + 32 * q;
-            if (q < nq && j < f) part[warp * f + j] = acc[q];
+            if (q < nq && j < f) wp[warp * f + j] = acc[q];
         }
         __syncthreads();
         for (int j = threadIdx.x; j < f; j += blockDim.x) {
-            T s = part[j];
-            for (int w = 1; w < ITEM_WARPS; ++w) s += part[w * f + j];
-            dY[it * f + j] = s;
+            T s = wp[j];
+            for (int w = 1; w < ITEM_WARPS; ++w) s += wp[w * f + j];
+            part[ch * f + j] = s;
         }
         __syncthreads();
+    }
+}
+
+// dY[i] = the item's chunk partials added in chunk order (first[i] .. first[i + 1]).
+template <typename T>
+__global__ void adjoint_combine_kernel(int64_t n, int f, const int32_t *__restrict__ first,
+                                       const T *__restrict__ part, T *__restrict__ dY) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * f;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / f;
+        const int j = (int)(e - i * f);
+        T s = T(0);
+        for (int32_t c = first[i]; c < first[i + 1]; ++c) s += part[(int64_t)c * f + j];
+        dY[e] = s;
     }
 }
 
@@ -350,10 +393,27 @@ als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T
     std::vector<float> hval_u, hval_i;
     group_by(m, nh, held->row_idxs, held->col_idxs, held->vals, hptr_u, hcol_u, hval_u);
     group_by(n, nh, held->col_idxs, held->row_idxs, held->vals, hptr_i, hrow_i, hval_i);
+    // chunks of at most ITEM_CHUNK training ratings per item (one for an item without any)
+    const std::vector<int32_t> &cp = h->host_ptr[1];
+    std::vector<int32_t> citem, cbeg, cend, cfirst((size_t)n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        cfirst[i] = (int32_t)citem.size();
+        const int32_t b = cp[i], e = cp[i + 1];
+        int32_t s = b;
+        do {
+            citem.push_back((int32_t)i);
+            cbeg.push_back(s);
+            cend.push_back(std::min(e, s + ITEM_CHUNK));
+            s += ITEM_CHUNK;
+        } while (s < e);
+    }
+    cfirst[n] = (int32_t)citem.size();
+    const int64_t nchunks = (int64_t)citem.size();
     cudaStream_t st = h->stream;
     int32_t *d_hptr_u = nullptr, *d_hcol_u = nullptr, *d_hptr_i = nullptr, *d_hrow_i = nullptr;
     float *d_hval_u = nullptr, *d_hval_i = nullptr;
-    T *d_X = nullptr, *d_G = nullptr, *d_dY = nullptr;
+    T *d_X = nullptr, *d_G = nullptr, *d_dY = nullptr, *d_part = nullptr;
+    int32_t *d_chunks = nullptr;  // citem, cbeg, cend (nchunks each), cfirst (n + 1)
     double *d_parts = nullptr;
     cudaError_t e = cudaSuccess;
     auto step = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
@@ -368,6 +428,8 @@ als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T
     step(cudaMalloc(&d_G, sizeof(T) * (size_t)(m * f)));
     step(cudaMalloc(&d_dY, sizeof(T) * (size_t)(n * f)));
     step(cudaMalloc(&d_parts, sizeof(double) * (size_t)(2 * m + 2)));
+    step(cudaMalloc(&d_chunks, sizeof(int32_t) * (size_t)(3 * nchunks + n + 1)));
+    step(cudaMalloc(&d_part, sizeof(T) * (size_t)(nchunks * f + 1)));
     if (e == cudaSuccess) {
         step(cudaMemcpyAsync(d_hptr_u, hptr_u.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
         step(cudaMemcpyAsync(d_hcol_u, hcol_u.data(), sizeof(int32_t) * nhp, cudaMemcpyHostToDevice, st));
@@ -375,6 +437,10 @@ als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T
         step(cudaMemcpyAsync(d_hptr_i, hptr_i.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
         step(cudaMemcpyAsync(d_hrow_i, hrow_i.data(), sizeof(int32_t) * nhp, cudaMemcpyHostToDevice, st));
         step(cudaMemcpyAsync(d_hval_i, hval_i.data(), sizeof(float) * nhp, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_chunks, citem.data(), sizeof(int32_t) * nchunks, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_chunks + nchunks, cbeg.data(), sizeof(int32_t) * nchunks, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_chunks + 2 * nchunks, cend.data(), sizeof(int32_t) * nchunks, cudaMemcpyHostToDevice, st));
+        step(cudaMemcpyAsync(d_chunks + 3 * nchunks, cfirst.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
         step(cudaMemsetAsync(h->d_flags, 0, sizeof(int32_t) * 4, st));
         AdjArgs<T> a{};
         a.ptr = h->d_csr_ptr;
@@ -399,11 +465,14 @@ als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T
         if (e == cudaSuccess && m > 0) adjoint_row_kernel<T><<<(unsigned)m, nt_of(FP), smem, st>>>(a, FP);
         step(cudaGetLastError());
         const size_t ismem = sizeof(T) * ITEM_WARPS * (size_t)f;
-        if (e == cudaSuccess && n > 0)
-            adjoint_item_kernel<T><<<(unsigned)std::min<int64_t>(n, 152 * 16), 32 * ITEM_WARPS,
-                                     ismem, st>>>(n, f, h->d_csc_ptr, h->d_csc_idx, h->d_csc_val,
-                                                  d_hptr_i, d_hrow_i, d_hval_i, d_Y, d_X, d_G,
-                                                  d_dY);
+        if (e == cudaSuccess && n > 0) {
+            adjoint_chunk_kernel<T><<<(unsigned)std::min<int64_t>(nchunks, 152 * 8),
+                                      32 * ITEM_WARPS, ismem, st>>>(
+                nchunks, f, d_chunks, d_chunks + nchunks, d_chunks + 2 * nchunks, h->d_csc_idx,
+                h->d_csc_val, d_hptr_i, d_hrow_i, d_hval_i, d_Y, d_X, d_G, d_part);
+            adjoint_combine_kernel<T><<<(unsigned)std::min<int64_t>((n * f + 255) / 256, 152 * 16),
+                                        256, 0, st>>>(n, f, d_chunks + 3 * nchunks, d_part, d_dY);
+        }
         step(cudaGetLastError());
         sum_doubles_kernel<<<1, 256, 0, st>>>(d_parts, m, d_parts + 2 * m);
         sum_doubles_kernel<<<1, 256, 0, st>>>(d_parts + m, m, d_parts + 2 * m + 1);
@@ -420,7 +489,8 @@ als_status adjoint_impl(als_handle *h, const als_coo_view *held, const T *d_Y, T
         if (loss) *loss = out[0];
         if (dLdlambda) *dLdlambda = out[1];
     }
-    void *all[] = {d_hptr_u, d_hcol_u, d_hval_u, d_hptr_i, d_hrow_i, d_hval_i, d_X, d_G, d_dY, d_parts};
+    void *all[] = {d_hptr_u, d_hcol_u, d_hval_u, d_hptr_i, d_hrow_i, d_hval_i, d_X, d_G, d_dY,
+                   d_parts, d_chunks, d_part};
     for (void *p : all)
         if (p) cudaFree(p);
     if (e != cudaSuccess) {

@@ -70,21 +70,16 @@ __global__ void quantise_bf16_kernel(const float *__restrict__ Y, int64_t rows, 
 // scale per row and column of every Gram, applied when the solver reads the accumulator.
 __global__ void colmax_kernel(const float *__restrict__ Y, int64_t rows, int f,
                               unsigned int *__restrict__ cmax) {
-    __shared__ unsigned int sm[MAXF];
-    for (int j = threadIdx.x; j < MAXF; j += blockDim.x) sm[j] = 0u;
-    __syncthreads();
-    const int64_t total = rows * (int64_t)f;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int j = (int)(e % f);
-        const float a = fabsf(Y[e]);
-        // non-negative floats order as their bit patterns; NaN (above +inf) surfaces as a NaN
-        // scale, whose rows the solver flags as non-finite
-        atomicMax(&sm[j], __float_as_uint(a));
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < f; j += blockDim.x)
-        if (sm[j]) atomicMax(&cmax[j], sm[j]);
+    // thread j of a block keeps column j's running maximum over the block's rows (a row's f
+    // values are consecutive: coalesced), then one atomic per block and column; non-negative
+    // floats order as their bit patterns, and a NaN (above +inf) surfaces as a NaN scale, whose
+    // rows the solver flags as non-finite
+    const int j = threadIdx.x;
+    if (j >= f) return;
+    unsigned int mx = 0u;
+    for (int64_t r = blockIdx.x; r < rows; r += gridDim.x)
+        mx = max(mx, __float_as_uint(fabsf(Y[r * f + j])));
+    if (mx) atomicMax(&cmax[j], mx);
 }
 
 // The scale exponent of a column from the bit pattern of its largest magnitude.
@@ -307,7 +302,9 @@ als_status tc_quantise(als_handle *h, int side, int *launches, std::string *why)
             1, std::min<int64_t>((opp * h->f + 255) / 256, (int64_t)t->num_sms * 8));
         cudaError_t e = cudaMemsetAsync(t->d_cmax, 0, sizeof(unsigned int) * tcg::MAXF, h->stream);
         if (e == cudaSuccess) {
-            tcg::colmax_kernel<<<grid, 256, 0, h->stream>>>(Y, opp, h->f, t->d_cmax);
+            const int cgrid =
+                (int)std::max<int64_t>(1, std::min<int64_t>(opp, (int64_t)t->num_sms * 16));
+            tcg::colmax_kernel<<<cgrid, tcg::MAXF, 0, h->stream>>>(Y, opp, h->f, t->d_cmax);
             tcg::quantise_e4m3_kernel<<<grid, 256, 0, h->stream>>>(Y, opp, h->f, t->d_cmax,
                                                                    t->d_scale[side], t->d_f8[side]);
             *launches += 2;

@@ -17,17 +17,7 @@ namespace als {
 namespace tcg {
 
 constexpr int KC = 64;                       // ratings per stage
-constexpr int MAX_NSTAGE = 8;
-// Stage-ring depth per solver: CG keeps no factor in shared memory, so its ring is deeper (more
-// gathered bytes in flight per SM; five stages beside the quad-blocked rows at FP = 112); the LU
-// scratch leaves room for five stages, and so does the Cholesky's except at FP = 112, where four
-// factor groups share the SM.  The tensor-core CG keeps only a 7 KB operand tile per group: eight
-// stages at FP <= 112 (measured 1-2% faster than six).
-__host__ __device__ constexpr int nstage_of(int solver, int fp) {
-    return solver == 3 ? (fp <= 112 ? 8 : 6)
-           : solver == 0 ? (fp == 112 ? 5 : 8)
-                         : (solver == 1 && fp == 112) ? 4 : 5;
-}
+constexpr int MAX_NSTAGE = 16;
 // CG at FP = 112 quad-blocks its rows (cg_quad): half of a row's values in registers, half in
 // shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups fit an SM.
 __host__ __device__ constexpr bool cg_quad_rows(int solver, int fp) { return solver == 0 && fp == 112; }
@@ -37,6 +27,11 @@ constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feat
 constexpr int TILE_BYTES = 2 * ATOM_STRIDE;  // 128 features
 constexpr int R_BYTES = 2 * ATOM_BYTES;      // K-major rating tile, N = 16 rows x 64 ratings
 constexpr int STAGE_BYTES = TILE_BYTES + R_BYTES;
+// FP8 stages: one 128-feature atom of KC ratings (8 KB) and the rating tile
+constexpr int TILE_BYTES_F8 = ATOM_STRIDE;
+constexpr int STAGE_BYTES_F8 = TILE_BYTES_F8 + R_BYTES;
+__host__ __device__ constexpr int stage_bytes(bool f8) { return f8 ? STAGE_BYTES_F8 : STAGE_BYTES; }
+__host__ __device__ constexpr int tile_bytes(bool f8) { return f8 ? TILE_BYTES_F8 : TILE_BYTES; }
 constexpr int MAXF = 128;
 constexpr int MAX_NBUF = 4;
 // Producer metadata ring: each stage's column ids and ratings are copied into shared memory MD
@@ -150,13 +145,29 @@ inline int fp_of(int f) {
     return r <= 32 ? 32 : r <= 64 ? 64 : r <= 112 ? 112 : 128;
 }
 
-constexpr size_t group_floats(int fp, int solver) {
-    const size_t vec = 2 * (size_t)fp + 16 + 5 * 128 + 64;
-    const size_t tri = 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp;
-    return solver == 0   ? (cg_quad_rows(solver, fp) ? (size_t)cgq_floats(fp) + 2 * (size_t)fp + 16 : vec)
-           : solver == 1 ? tri + 8 * (size_t)fp + vec
-           : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + vec + 31) / 32 * 32
-                         : (size_t)fp * (fp + 4) + 8 * (size_t)fp + vec;
+__host__ __device__ constexpr size_t group_floats(int fp, int solver) {
+    return solver == 0   ? (cg_quad_rows(solver, fp)
+                                ? (size_t)cgq_floats(fp) + 2 * (size_t)fp + 16
+                                : 2 * (size_t)fp + 16 + 5 * 128 + 64)
+           : solver == 1 ? 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp + 8 * (size_t)fp +
+                               2 * (size_t)fp + 16 + 5 * 128 + 64
+           : solver == 3 ? ((size_t)cgtc_tile_floats(fp) + 2 * (size_t)fp + 16 + 5 * 128 + 64 + 31) /
+                               32 * 32
+                         : (size_t)fp * (fp + 4) + 8 * (size_t)fp + 2 * (size_t)fp + 16 + 5 * 128 + 64;
+}
+// Stage-ring depth: as many stages as the shared memory left beside the solver groups' scratch,
+// the metadata ring and the barriers holds (at most MAX_NSTAGE).  On Gram-bound rows a stage's
+// life (gather issue, the rows' L2 round trip, the MMAs, the commit that frees the slot) is
+// long against its MMA time, so the stages in flight set the rate; on solve-bound rows more
+// stages cost nothing (one CTA per SM).  FP8 stages are 10 KB instead of 18 KB.
+constexpr size_t SMEM_BUDGET = 232448 - 2048;  // the opt-in limit per CTA, less alignment slack
+__host__ __device__ constexpr int nstage_fit(int solver, int fp, bool f8) {
+    return (int)((SMEM_BUDGET - sizeof(float) * group_floats(fp, solver) * nepi_of(solver, fp) -
+                  (size_t)MRING_BYTES - 1024 - (f8 ? sizeof(float) * MAXF : 0)) /
+                 (size_t)stage_bytes(f8));
+}
+__host__ __device__ constexpr int nstage_of(int solver, int fp, bool f8) {
+    return nstage_fit(solver, fp, f8) > MAX_NSTAGE ? MAX_NSTAGE : nstage_fit(solver, fp, f8);
 }
 
 inline Geometry geometry(int f, int solver, bool f8 = false) {
@@ -172,8 +183,8 @@ inline Geometry geometry(int f, int solver, bool f8 = false) {
     g.nepi = nepi_of(solver, g.fp);
     g.tmem_cols = g.nbuf * g.acc_stride;
     g.nthreads = nthreads_of(solver, g.fp);
-    const int ns = nstage_of(solver, g.fp);
-    size_t bytes = (size_t)ns * STAGE_BYTES;                         // operand ring
+    const int ns = nstage_of(solver, g.fp, f8);
+    size_t bytes = (size_t)ns * stage_bytes(f8);                     // operand ring
     bytes += sizeof(float) * group_floats(g.fp, solver) * g.nepi;    // per-group scratch
     if (f8) bytes += sizeof(float) * MAXF;                            // per-feature scales
     bytes += MRING_BYTES;                                            // metadata ring
@@ -858,7 +869,9 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 template <int FP, int SOLVER, bool F8>
 __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     sweep_tc_kernel(const __grid_constant__ Params p) {
-    constexpr int NSTAGE = nstage_of(SOLVER, FP);
+    constexpr int NSTAGE = nstage_of(SOLVER, FP, F8);
+    constexpr int SBYTES = stage_bytes(F8), TBYTES = tile_bytes(F8);
+    static_assert(NSTAGE >= 2 && NSTAGE <= MAX_NSTAGE, "stage ring");
     constexpr int NEPI = nepi_of(SOLVER, FP);
     constexpr int WP = 4 * NEPI;  // producer warp; then the MMA issuer and the gather warps
     constexpr int WM = WP + 1;
@@ -875,7 +888,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
-    float *gscratch = (float *)(ring + NSTAGE * STAGE_BYTES);
+    float *gscratch = (float *)(ring + NSTAGE * SBYTES);
     float *dsc = gscratch + GroupLayout<FP, SOLVER>::floats * NEPI;  // [MAXF] FP8 scales
     int32_t *mcol = (int32_t *)(dsc + (F8 ? MAXF : 0));                             // [MR][KC]
     float *mval = reinterpret_cast<float *>(mcol + MR * KC);                            // [MR][KC]
@@ -902,7 +915,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     const int nbuf = p.nbuf;
 
     // zero the operand ring once: features f..127 and rating-tile rows 1..15 are never written
-    for (int i = tid; i < NSTAGE * STAGE_BYTES / 16; i += blockDim.x)
+    for (int i = tid; i < NSTAGE * SBYTES / 16; i += blockDim.x)
         reinterpret_cast<uint4 *>(ring)[i] = make_uint4(0, 0, 0, 0);
     if constexpr (SOLVER == SOLVER_CGTC) {  // the groups' operand tiles: columns 2..15 stay zero
         for (int i = tid; i < (int)(GroupLayout<FP, SOLVER>::floats * NEPI / 4); i += blockDim.x)
@@ -1130,7 +1143,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 if ((m.flags & 1) && !take_buffer()) { ok = false; break; }
                 const uint32_t dg = tmem_base + buf * p.acc_stride;
                 const uint32_t db = dg + p.ng;
-                const uint32_t tile_s = ring_s + s * STAGE_BYTES;
+                const uint32_t tile_s = ring_s + s * SBYTES;
                 if constexpr (F8) {
                     // K = 32 ratings (four 8-rating groups, 4 KB of the one-atom panel) and the
                     // matching 32 bytes of the rating tile's row per MMA
@@ -1140,7 +1153,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                             sdesc(tile_s + kk * 4 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
                         const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
                         mma_e4m3(dg, ad, ad, idesc_g, accum);
-                        const uint64_t rd = sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                        const uint64_t rd = sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
                         mma_e4m3(db, ad, rd, idesc_r, accum);
                     }
                 } else {
@@ -1152,7 +1165,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                         mma_bf16(dg, ad, ad, idesc_g, accum);
                         if (!FUSED) {
                             const uint64_t rd =
-                                sdesc(tile_s + TILE_BYTES + kk * 32, 16, ATOM_BYTES);
+                                sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
                             mma_bf16(db, ad, rd, idesc_r, accum);
                         }
                     }
@@ -1321,10 +1334,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                 m.flags = __shfl_sync(0xffffffffu, w.z, 0);
                 m.nu = __shfl_sync(0xffffffffu, w.w, 0);
             }
-            uint8_t *tile = ring + s * STAGE_BYTES;
-            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TILE_BYTES);
+            uint8_t *tile = ring + s * SBYTES;
+            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TBYTES);
             if constexpr (F8) {  // e4m3 ratings (star ratings are exact), bytes 0..63 of row 0
-                uint8_t *rt8 = tile + TILE_BYTES;
+                uint8_t *rt8 = tile + TBYTES;
                 rt8[lane] = __nv_cvt_float_to_fp8(mval[slot * KC + lane], __NV_SATFINITE, __NV_E4M3);
                 rt8[lane + 32] =
                     __nv_cvt_float_to_fp8(mval[slot * KC + lane + 32], __NV_SATFINITE, __NV_E4M3);

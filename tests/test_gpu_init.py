@@ -1,5 +1,5 @@
 """The srand(0) factor initialisation (als_model.cu:1772-1784) generated on the GPU: glibc's
-rand() sequence by jump-ahead, one thread per block of 15,872 calls.  Bit-exact against the
+rand() sequence by jump-ahead, one thread per block of 1,984 calls.  Bit-exact against the
 oracle, which calls the C library's srand(0) / rand() itself, at sizes around the block edges
 and at workload 4's full table (480,189 x 128 = 61.5M calls)."""
 from __future__ import annotations
@@ -12,11 +12,11 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-S = 31 * 512
+S = 31 * 64  # rand() calls per GPU thread
 
 
 @pytest.mark.parametrize("n,f", [(1, 1), (7, 5), (1, 30), (1, 31), (1, 32), (S - 1, 1), (S, 1),
-                                 (S + 1, 1), (64, 2 * S // 64 + 3), (480189, 128)])
+                                 (S + 1, 1), (1000, 33), (3 * S + 5, 1), (480189, 128)])
 def test_gpu_init_is_the_c_library_sequence(n, f):
     m = 3
     ptr = np.array([0, 1, 1, 2], np.int32)
