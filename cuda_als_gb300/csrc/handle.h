@@ -72,6 +72,17 @@ struct als_handle {
 
     TcState *tc = nullptr;
 
+    // FP32 path: the heavy rows' parts per side (built on the side's first FP32 sweep, dropped
+    // when the ratings change): device tables part_beg, part_end, first (one block), the host
+    // copy of `first`, and the partial-Gram scratch
+    struct Split {
+        bool built = false;
+        int32_t nheavy = 0, nparts = 0;
+        int32_t *d_tab = nullptr;
+        std::vector<int32_t> first;
+        float *d_part = nullptr;
+    } split[2];
+
     // event log attached by als_set_log (not owned): training lines, per-iteration test RMSE
     als_log *log = nullptr;
     bool log_iter_rmse = false, log_cout = false;

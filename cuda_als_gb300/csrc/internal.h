@@ -110,9 +110,23 @@ struct SweepArgs {
     int32_t *flags;         // [0] flagged rows (atomic), [1] fp64-refined rows
 };
 
-// Fused FP32 Gram + RHS + solve, one CTA per row (sweep_fp32.cu).
+// Rows of the FP32 path heavier than FP32_SPLIT_RATINGS ratings: each split into parts of that
+// many ratings whose partial Grams separate CTAs build, then added in order by one CTA per row
+// that solves it.  The heavy rows are the first `nheavy` positions of the side's order.
+constexpr int32_t FP32_SPLIT_RATINGS = 16384;
+struct Fp32Split {
+    const int32_t *part_beg = nullptr, *part_end = nullptr;  // device, per part
+    const int32_t *first = nullptr;       // device, nheavy + 1: first part of each heavy row
+    const int32_t *first_host = nullptr;  // host copy of `first`
+    int32_t nheavy = 0;
+    float *part = nullptr;                // parts x fp32_part_floats(f)
+};
+size_t fp32_part_floats(int f);
+
+// Fused FP32 Gram + RHS + solve, one CTA per row (sweep_fp32.cu), heavy rows split.
 bool fp32_supported(int f);
-cudaError_t launch_sweep_fp32(const SweepArgs &a, cudaStream_t st, int *launches);
+cudaError_t launch_sweep_fp32(const SweepArgs &a, const Fp32Split *sp, cudaStream_t st,
+                              int *launches);
 
 // ---------------------------------------------------------------------------------------------
 // Evaluation (rmse.cu)

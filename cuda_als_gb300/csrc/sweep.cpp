@@ -7,6 +7,7 @@
 // is handled by fused kernels in descending-degree order with no host round trip.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -42,7 +43,10 @@ als_status prepare_precision_path(als_handle *h) {
     return ALS_OK;
 }
 
+void release_split(als_handle *h);
+
 void release_precision_path(als_handle *h) {
+    release_split(h);
     for (int s = 0; s < 2; ++s)
         for (int k = 0; k < 2; ++k)
             if (h->ev_half[s][k]) cudaEventDestroy(h->ev_half[s][k]);
@@ -135,6 +139,7 @@ static void build_plan(als_handle *h, int side) {
 void data_changed(als_handle *h) {
     invalidate_graphs(h);
     for (auto &pl : h->plan) pl.clear();
+    release_split(h);
 }
 
 // Forget the autotuner's decisions (als_init_factors with autotune = 1).
@@ -154,10 +159,63 @@ static bool plan_final(const als_handle *h) {
     return true;
 }
 
+void release_split(als_handle *h) {
+    for (auto &sp : h->split) {
+        if (sp.d_tab) cudaFree(sp.d_tab);
+        if (sp.d_part) cudaFree(sp.d_part);
+        sp = als_handle::Split();
+    }
+}
+
+// The FP32 path's heavy rows of a side (degree > FP32_SPLIT_RATINGS): the first positions of the
+// side's descending-degree order (ties by ascending row id, the order the device sort makes),
+// each cut into parts of FP32_SPLIT_RATINGS ratings.
+static cudaError_t build_split(als_handle *h, int side) {
+    als_handle::Split &sp = h->split[side];
+    if (sp.built) return cudaSuccess;
+    const std::vector<int32_t> &ptr = h->host_ptr[side];
+    const int64_t rows = (int64_t)ptr.size() - 1;
+    std::vector<int32_t> heavy;
+    for (int64_t r = 0; r < rows; ++r)
+        if (ptr[r + 1] - ptr[r] > FP32_SPLIT_RATINGS) heavy.push_back((int32_t)r);
+    std::stable_sort(heavy.begin(), heavy.end(), [&](int32_t x, int32_t y) {
+        return ptr[x + 1] - ptr[x] > ptr[y + 1] - ptr[y];
+    });
+    std::vector<int32_t> pbeg, pend;
+    sp.first.assign(1, 0);
+    for (int32_t r : heavy) {
+        for (int32_t b = ptr[r]; b < ptr[r + 1]; b += FP32_SPLIT_RATINGS) {
+            pbeg.push_back(b);
+            pend.push_back(std::min(ptr[r + 1], b + FP32_SPLIT_RATINGS));
+        }
+        sp.first.push_back((int32_t)pbeg.size());
+    }
+    sp.nheavy = (int32_t)heavy.size();
+    sp.nparts = (int32_t)pbeg.size();
+    if (sp.nparts > 0) {
+        const size_t np = (size_t)sp.nparts;
+        cudaError_t e = cudaMalloc(&sp.d_tab, sizeof(int32_t) * (2 * np + sp.first.size()));
+        if (e == cudaSuccess)
+            e = cudaMalloc(&sp.d_part, sizeof(float) * np * fp32_part_floats(h->f));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sp.d_tab, pbeg.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sp.d_tab + np, pend.data(), sizeof(int32_t) * np, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sp.d_tab + 2 * np, sp.first.data(), sizeof(int32_t) * sp.first.size(),
+                           cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+    }
+    sp.built = true;
+    return cudaSuccess;
+}
+
 static cudaError_t launch_bucket(als_handle *h, int side, const SweepBucket &b, int solve, int slot,
                                  int *launches) {
     if (h->precision != ALS_PREC_FP32)
         return tc_launch_bucket(h, side, b.lo, b.hi, solve, slot, launches);
+    cudaError_t e = build_split(h, side);
+    if (e != cudaSuccess) return e;
     SweepArgs a{};
     a.ptr = side == 0 ? h->d_csr_ptr : h->d_csc_ptr;
     a.idx = side == 0 ? h->d_csr_idx : h->d_csc_idx;
@@ -173,7 +231,18 @@ static cudaError_t launch_bucket(als_handle *h, int side, const SweepBucket &b, 
     a.cg_iters = h->cfg.cg_steps;
     a.cg_tol = h->cfg.cg_tol;
     a.flags = h->d_flags;
-    return launch_sweep_fp32(a, h->stream, launches);
+    const als_handle::Split &sp = h->split[side];
+    Fp32Split fs;
+    if (sp.nparts > 0) {
+        const size_t np = (size_t)sp.nparts;
+        fs.part_beg = sp.d_tab;
+        fs.part_end = sp.d_tab + np;
+        fs.first = sp.d_tab + 2 * np;
+        fs.first_host = sp.first.data();
+        fs.nheavy = sp.nheavy;
+        fs.part = sp.d_part;
+    }
+    return launch_sweep_fp32(a, sp.nparts > 0 ? &fs : nullptr, h->stream, launches);
 }
 
 // The tuning sweep of a side (ALS_SOLVE_AUTO, the side's second half-sweep: the first leaves the

@@ -344,3 +344,31 @@ def test_gpu_empty_rows_and_columns_solve_to_zero():
         assert not mdl.h_UT[[0, 7, 59]].any()
         assert not mdl.h_VT[3].any()
         assert np.isfinite(mdl.h_UT).all() and np.isfinite(mdl.h_VT).all()
+
+
+@pytest.mark.parametrize("f,solve", [(64, ca.SOLVE_TYPE.CHOLESKY), (100, ca.SOLVE_TYPE.LU),
+                                     (100, ca.SOLVE_TYPE.CUMF_ALS_CG_FP32)])
+def test_fp32_rows_split_into_parts_match_the_oracle(f, solve):
+    """Rows above 16,384 ratings run as parts (partial Grams by separate CTAs, added in order):
+    degrees on both sides of the threshold, a row of 50k ratings, light rows beside them."""
+    rng = np.random.default_rng(f)
+    m, n = 8, 60000
+    degrees = np.array([50000, 40000, 16385, 16384, 16383, 100, 3, 0])
+    ptr, idx, val = random_csr(rng, m, n, degrees=degrees)
+    V0 = (rng.standard_normal((n, f)) * 0.1).astype(np.float32)
+    U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
+    tr = ca.host_sparse_matrix(m, n, len(idx)).set_csr(ptr, idx, val)
+    with ca.als_model(tr, None, f, 0.05, 1, ca.CALCULATE_VTVS_TYPE.SIMPLE, solve,
+                      precision=int(ca.PRECISION.FP32), cg_tol=0.0) as mdl:
+        mdl.set_factors(U0, V0)
+        mdl.half_sweep(0)
+        U, _ = mdl.get_factors()
+        assert mdl.counters()["flagged_rows"] == 0
+    osolve = {ca.SOLVE_TYPE.CHOLESKY: O.CHOLESKY, ca.SOLVE_TYPE.LU: O.LU,
+              ca.SOLVE_TYPE.CUMF_ALS_CG_FP32: O.CG_FP32}[solve]
+    Ue = U0.copy()
+    O.half_sweep(ptr, idx, val, V0, Ue, f, 0.05, solve=osolve, cg_tol=0.0)
+    num = np.linalg.norm(U.astype(np.float64) - Ue, axis=1)
+    den = np.maximum(np.linalg.norm(Ue.astype(np.float64), axis=1), 1e-6)
+    assert (num / den).max() < (1e-4 if osolve != O.CG_FP32 else 1e-3)
+    assert not U[-1].any()
