@@ -40,6 +40,23 @@ __device__ __forceinline__ float gsum128(float v, float *red, int &slot, const G
     return (r[0] + r[1]) + (r[2] + r[3]);
 }
 
+// Two fixed-order sums over the 128 threads in one pass (one barrier); `red` as for gsum128 (the
+// two values of a warp share a float2 of the same ring slot: 4 x 8 floats).
+__device__ __forceinline__ float2 gsum128x2(float u, float v, float *red, int &slot,
+                                            const GroupSync &gs) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        u += __shfl_xor_sync(0xffffffffu, u, o);
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    float2 *r = reinterpret_cast<float2 *>(red) + 4 * (slot & 3);
+    ++slot;
+    if ((threadIdx.x & 31) == 0) r[((threadIdx.x >> 5) & 3)] = make_float2(u, v);
+    gs.sync();
+    const float2 a = r[0], b = r[1], c = r[2], d = r[3];
+    return make_float2((a.x + b.x) + (c.x + d.x), (a.y + b.y) + (c.y + d.y));
+}
+
 __device__ __forceinline__ float gmax128(float v, float *red, int &slot, const GroupSync &gs) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -66,9 +83,57 @@ __device__ __forceinline__ float dot_row(const float (&a)[FP], const float *sv) 
     return (s0 + s1) + (s2 + s3);
 }
 
+// CG with one reduction per iteration (Chronopoulos and Gear, 1989): with w = A r, the two dot
+// products gamma = r'r and delta = r'w are summed together, and p'Ap = delta - beta gamma / alpha
+// follows from the recurrences.  In exact arithmetic the iterates are those of the reference's
+// CG (cumf_als_cg/cg.cu:37-232, warm start, at most `iters` updates, exit when r'r < tol after an
+// update, stop before an update whose p'Ap is not positive); a product of A follows every update
+// but the last, so without an early exit it performs the same iters + 1 products, with one
+// barrier and one two-value reduction per iteration instead of three barriers and two
+// reductions.  `mul(v)` returns (A v)_i after publishing v_i to the group (it synchronises).
+template <class Mul>
+__device__ __forceinline__ float cg_single_reduction(Mul mul, float bi, float xi, float *red,
+                                                     int iters, float tol, const GroupSync &gs) {
+    int slot = 0;
+    float r = bi - mul(xi);
+    gs.sync();  // every thread has read x out of the shared vector before r overwrites it
+    float w = mul(r);
+    float2 gd = gsum128x2(r * r, r * w, red, slot, gs);
+    float gamma = gd.x, pap = gd.y;
+    float p = r, s = w, alpha = 0.f;
+    for (int it = 0; it < iters; ++it) {
+        if (!(pap > 0.f)) break;
+        alpha = gamma / pap;
+        xi = fmaf(alpha, p, xi);
+        r = fmaf(-alpha, s, r);
+        if (it + 1 == iters) break;  // no further update: the product would be unused
+        w = mul(r);
+        gd = gsum128x2(r * r, r * w, red, slot, gs);
+        if (gd.x < tol) break;
+        const float beta = gd.x / gamma;
+        pap = gd.y - beta * gd.x / alpha;  // p_new' A p_new
+        gamma = gd.x;
+        p = fmaf(beta, p, r);
+        s = fmaf(beta, s, w);
+    }
+    return xi;
+}
+
 template <int FP>
 __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *sv, float *red,
                         int iters, float tol, const GroupSync &gs) {
+    const bool live = i < FP;  // threads past the padded size hold zero rows and write nothing
+    auto mul = [&](float v) -> float {
+        if (live) sv[i] = v;  // every thread finished reading sv at the previous reduction
+        gs.sync();
+        return dot_row<FP>(a, sv);
+    };
+    return cg_single_reduction(mul, bi, xi, red, iters, tol, gs);
+}
+
+template <int FP>
+__device__ float cg_reg_two_reductions(const float (&a)[FP], float bi, float xi, int i, float *sv,
+                                       float *red, int iters, float tol, const GroupSync &gs) {
     int slot = 0;
     const bool live = i < FP;  // threads past the padded size hold zero rows and write nothing
     if (live) sv[i] = xi;
@@ -137,6 +202,20 @@ __device__ __forceinline__ float dot_quad(const float4 (&ar)[2][NK], const float
 template <int NK>
 __device__ float cg_quad(const float4 (&ar)[2][NK], const float4 *sa, float bi, float xi, int i,
                          float *sv, float *red, int iters, float tol, const GroupSync &gs) {
+    constexpr int FP = 16 * NK;
+    const bool live = i < FP;
+    auto mul = [&](float v) -> float {
+        if (live) sv[i] = v;
+        gs.sync();
+        return dot_quad<NK>(ar, sa, sv, i);
+    };
+    return cg_single_reduction(mul, bi, xi, red, iters, tol, gs);
+}
+
+template <int NK>
+__device__ float cg_quad_two_reductions(const float4 (&ar)[2][NK], const float4 *sa, float bi,
+                                        float xi, int i, float *sv, float *red, int iters,
+                                        float tol, const GroupSync &gs) {
     constexpr int FP = 16 * NK;
     int slot = 0;
     const bool live = i < FP;

@@ -123,7 +123,7 @@ struct GroupLayout {
     // the quad-blocked CG needs no vectors past the reduction ring)
     static constexpr size_t floats =
         SOLVER == 3 ? (ls_floats + 2 * FP + 16 + 5 * 128 + 64 + 31) / 32 * 32
-        : cg_quad_rows(SOLVER, FP) ? ls_floats + 2 * FP + 16
+        : cg_quad_rows(SOLVER, FP) ? ls_floats + 2 * FP + 32
                                    : ls_floats + 2 * FP + 16 + 5 * 128 + 64;
 };
 
@@ -147,7 +147,7 @@ inline int fp_of(int f) {
 
 __host__ __device__ constexpr size_t group_floats(int fp, int solver) {
     return solver == 0   ? (cg_quad_rows(solver, fp)
-                                ? (size_t)cgq_floats(fp) + 2 * (size_t)fp + 16
+                                ? (size_t)cgq_floats(fp) + 2 * (size_t)fp + 32
                                 : 2 * (size_t)fp + 16 + 5 * 128 + 64)
            : solver == 1 ? 32 * (size_t)(fp / 8) * (fp / 8 + 1) + 4 * (size_t)fp + 8 * (size_t)fp +
                                2 * (size_t)fp + 16 + 5 * 128 + 64
@@ -602,8 +602,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     float *Ls = gsm;
     float *sv = gsm + GroupLayout<FP, SOLVER>::ls_floats;
     float *yv = sv + FP;
-    float *red = yv + FP;
-    float *vec = red + 16;  // 5 x 128 floats for the shared-memory solvers
+    float *red = yv + FP;   // reduction ring: 16 floats, 32 for the CGs' two-value sums
+    float *vec = red + 16;  // 5 x 128 floats for the shared-memory solvers (not the CGs)
     const int f = p.f;
     float *xo = p.X + (int64_t)m.row * f;
     const float reg = (float)m.nu * p.lambda;  // items_cnt * lambda (als_model.cu:157-159)
