@@ -882,8 +882,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     // (the gather left it zero: ng >= fst) and marks the stage ready; the MMA issuer waits for
     // ready and issues M=128 x N=ng+16 (Gram in columns [0, ng), b in column ng; row ng of the
     // accumulator then holds b^T, a padded row the solvers ignore).  Where the gather warps have
-    // the time: the tensor-core CG's six; FP = 128 (ng = 128) has no free column.
-    constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112 && !F8;
+    // the time: the tensor-core CG's six; FP = 128 (ng = 128) has no free column.  FP8 stages
+    // take the e4m3 rating into byte ng of each 128-byte row: one MMA per 32 ratings instead of
+    // a Gram MMA and an N = 16 right-hand-side MMA (the same e4m3 products, summed in one pass).
+    constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112;
     static_assert(NGATHER <= MAX_NGATHER, "");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -1104,8 +1106,9 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     } else if (warp == WM) {
         // ------------------------------------------------------------------ MMA issuer
         if (lane == 0) {
-            const uint32_t idesc_g = F8 ? idesc_e4m3(128, p.ng, true, true)
-                                        : idesc_bf16(128, FUSED ? p.ng + 16 : p.ng, true, true);
+            const int ng_mma = FUSED ? p.ng + 16 : p.ng;
+            const uint32_t idesc_g = F8 ? idesc_e4m3(128, ng_mma, true, true)
+                                        : idesc_bf16(128, ng_mma, true, true);
             const uint32_t idesc_r = F8 ? idesc_e4m3(128, 16, true, false)
                                         : idesc_bf16(128, 16, true, false);
             const uint32_t ring_s = smem_u32(ring);
@@ -1153,8 +1156,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                             sdesc(tile_s + kk * 4 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
                         const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
                         mma_e4m3(dg, ad, ad, idesc_g, accum);
-                        const uint64_t rd = sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
-                        mma_e4m3(db, ad, rd, idesc_r, accum);
+                        if (!FUSED) {
+                            const uint64_t rd = sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
+                            mma_e4m3(db, ad, rd, idesc_r, accum);
+                        }
                     }
                 } else {
                     const int nk = (m.cnt + 15) >> 4;
@@ -1381,11 +1386,21 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
                     ok = false;
                     break;
                 }
-                const int ra = p.ng >> 6, rc = (p.ng & 63) >> 3;  // column ng: atom, chunk
-                for (int k = lane; k < 4 * nq; k += 32)
-                    *reinterpret_cast<__nv_bfloat16 *>(tile + ra * ATOM_STRIDE +
-                                                       (k >> 3) * ATOM_BYTES + (k & 7) * 128 +
-                                                       ((rc ^ (k & 7)) << 4)) = rt[k];
+                if constexpr (F8) {
+                    // one 128-feature atom of bytes: column ng (a multiple of 16) starts
+                    // 16-byte chunk ng / 16 of each row, before the 128-byte swizzle
+                    const int rc = p.ng >> 4;
+                    const uint8_t *rt8 = tile + TBYTES;
+                    for (int k = lane; k < 4 * nq; k += 32)
+                        tile[(k >> 3) * ATOM_BYTES + (k & 7) * 128 + ((rc ^ (k & 7)) << 4)] =
+                            rt8[k];
+                } else {
+                    const int ra = p.ng >> 6, rc = (p.ng & 63) >> 3;  // column ng: atom, chunk
+                    for (int k = lane; k < 4 * nq; k += 32)
+                        *reinterpret_cast<__nv_bfloat16 *>(tile + ra * ATOM_STRIDE +
+                                                           (k >> 3) * ATOM_BYTES + (k & 7) * 128 +
+                                                           ((rc ^ (k & 7)) << 4)) = rt[k];
+                }
                 fence_async_smem();  // generic stores, read by the tensor core
                 __syncwarp();
                 if (lane == 0) mbar_arrive(smem_u32(&ready[s]));

@@ -67,9 +67,11 @@ def test_fp8_other_solvers(solve, f):
     assert rel_rows(U, Ue) < (TOL_BF16_INPUTS if osolve == O.LU else 1e-3)
 
 
-def test_fp8_cg16_on_general_factors():
-    """The FP16-Gram CG with its products on the tensor core, from an FP8 Gram (f = 128)."""
-    f = 128
+@pytest.mark.parametrize("f", [16, 64, 100, 112, 128])
+def test_fp8_cg16_on_general_factors(f):
+    """The FP16-Gram CG with its products on the tensor core, from an FP8 Gram.  Up to f = 112
+    the ratings ride in the Gram's MMA as feature column ng (one MMA per 32 ratings); at f = 128
+    there is no free column and the right-hand side takes its own N = 16 MMA."""
     rng, m, n, ptr, idx, val = stage_boundary_problem(f, seed=29)
     U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
     V0 = (rng.standard_normal((n, f)) * 0.3).astype(np.float32)
@@ -101,6 +103,28 @@ def test_fp8_heavy_rows_many_stages():
     Ue = np.zeros((m, f), np.float32)
     O.half_sweep(ptr, idx, val, quant.e4m3_table(V0)[0], Ue, f, 0.05, solve=O.CHOLESKY)
     assert rel_rows(U, Ue) < TOL_BF16_INPUTS
+
+
+def test_fp8_fused_rhs_on_heavy_rows():
+    """Rows of up to 5,999 ratings (94 stages) through the tensor-core CG at f = 100, where the
+    e4m3 ratings ride in the Gram's MMA as feature column 112."""
+    rng = np.random.default_rng(5)
+    m, n, f = 64, 6000, 100
+    degrees = rng.integers(1, 40, m)
+    degrees[:4] = [5999, 4096, 3000, 2049]
+    from conftest import random_csr
+    ptr, idx, val = random_csr(rng, m, n, degrees=degrees)
+    V0 = (rng.standard_normal((n, f)) * 0.2).astype(np.float32)
+    with make_model(m, n, ptr, idx, val, f, solve=ca.SOLVE_TYPE.CUMF_ALS_CG_FP16, cg_tol=0.0,
+                    precision=FP8) as mdl:
+        mdl.set_factors(np.zeros((m, f), np.float32), V0)
+        mdl.half_sweep(0)
+        U, _ = mdl.get_factors()
+    Ue = np.zeros((m, f), np.float32)
+    O.half_sweep(ptr, idx, val, quant.e4m3_table(V0)[0], Ue, f, 0.05, solve=O.CG_FP16,
+                 cg_tol=0.0)
+    d = np.asarray(U, np.float64) - Ue
+    assert np.linalg.norm(d) / np.linalg.norm(Ue) < 2e-3
 
 
 def test_fp8_training_on_the_transposed_netflix_shape():
