@@ -28,10 +28,17 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 2048
 constexpr int RADIX_BITS = 8;
 constexpr int RADIX_BINS = 1 << RADIX_BITS;  // 256 == threads per CTA
 constexpr int RADIX_THREADS = 256;
-constexpr int RADIX_WARPS = RADIX_THREADS / 32;
-constexpr int RADIX_ROUNDS = 16;                                 // keys per lane
+constexpr int RADIX_ROUNDS = 16;                                 // keys per lane (histogram)
 constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;          // 4096
-constexpr int RADIX_WARP_SPAN = 32 * RADIX_ROUNDS;                // 512 contiguous keys / warp
+// The scatter is latency-bound (each CTA loads its whole tile, ranks it, then writes it): it
+// runs the same 4,096-key tile with twice the threads and half the keys a lane, so that two
+// CTAs of 16 warps fit an SM within its registers (at 16 keys a lane, 99 registers held it to
+// two CTAs of 8 warps).
+constexpr int SCAT_THREADS = 512;
+constexpr int SCAT_WARPS = SCAT_THREADS / 32;                     // 16
+constexpr int SCAT_ROUNDS = RADIX_TILE / SCAT_THREADS;            // 8 keys per lane
+constexpr int SCAT_WARP_SPAN = 32 * SCAT_ROUNDS;                  // 256 contiguous keys / warp
+static_assert(SCAT_THREADS >= RADIX_BINS && RADIX_BINS % 32 == 0, "one thread per digit");
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -149,77 +156,89 @@ struct Payload {
     int pos_word;  // -1: none
 };
 
-// Stable scatter.  Warp w of tile t owns the contiguous key range [t*4096 + w*512, +512) and
-// walks it in 16 rounds of 32; a key's rank inside its warp is (keys of the same digit in
-// earlier rounds) + (lanes below it with the same digit in this round), found with match.any.
-// The warp offsets per digit are an exclusive prefix over warps, the tile's digit starts an
-// exclusive scan over digits.  The keys and their W payload words are first placed in shared
-// memory in digit order (the tile sorted by digit), then streamed out: consecutive threads write
+// Stable scatter.  Warp w of tile t owns the contiguous key range [t*4096 + w*256, +256) and
+// walks it in 8 rounds of 32; a key's rank inside its warp is (keys of the same digit in earlier
+// rounds) + (lanes below it with the same digit in this round), found with match.any.  The warp
+// offsets per digit are an exclusive prefix over warps, the tile's digit starts an exclusive
+// scan over digits.  The keys and their W payload words are first placed in shared memory in
+// digit order (the tile sorted by digit), then streamed out: consecutive threads write
 // consecutive addresses of a digit's run, so the global stores coalesce instead of scattering 32
 // ways per instruction.  A key's destination, goff[d] + (warp offset within d) + rank, is the
 // same either way (stable).  Dynamic shared memory: (1 + W) x RADIX_TILE words.
 template <int W>
-__global__ void __launch_bounds__(RADIX_THREADS)
+__global__ void __launch_bounds__(SCAT_THREADS, 2)
 radix_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ keys_out,
                      Payload pl, int64_t n, int shift, int64_t ntiles,
                      const int32_t *__restrict__ hist_scan) {
     extern __shared__ int32_t tile_words[];  // skey[RADIX_TILE], then W payload tiles
-    __shared__ int wcnt[RADIX_WARPS][RADIX_BINS];
+    __shared__ int wcnt[SCAT_WARPS][RADIX_BINS];
     __shared__ int goff[RADIX_BINS];
     __shared__ int tstart[RADIX_BINS];
-    __shared__ int wsum[RADIX_WARPS];
+    __shared__ int wsum[RADIX_BINS / 32];
     int32_t *skey = tile_words;
     int32_t *spay = tile_words + RADIX_TILE;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int w = 0; w < RADIX_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
-    goff[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+    const bool digit_thread = threadIdx.x < RADIX_BINS;  // whole warps: RADIX_BINS % 32 == 0
+    for (int i = threadIdx.x; i < SCAT_WARPS * RADIX_BINS; i += SCAT_THREADS) (&wcnt[0][0])[i] = 0;
+    if (digit_thread) goff[threadIdx.x] = hist_scan[(int64_t)threadIdx.x * ntiles + blockIdx.x];
     __syncthreads();
 
+    // tile-local 32-bit offsets (n <= INT32_MAX): one 64-bit base per array
     const int64_t tile0 = (int64_t)blockIdx.x * RADIX_TILE;
-    const int64_t base = tile0 + (int64_t)warp * RADIX_WARP_SPAN;
+    const int nvalid = (int)(n - tile0 < RADIX_TILE ? n - tile0 : RADIX_TILE);
+    const int32_t *kin = keys_in + tile0;
+    const int wbase = warp * SCAT_WARP_SPAN;
     const unsigned lt_mask = (1u << lane) - 1u;
-    int32_t key[RADIX_ROUNDS], pay[W][RADIX_ROUNDS];
-    int rank[RADIX_ROUNDS];
+    int32_t key[SCAT_ROUNDS], pay[W][SCAT_ROUNDS];
+    int rank[SCAT_ROUNDS];
 #pragma unroll
-    for (int q = 0; q < RADIX_ROUNDS; ++q) {
-        int64_t pos = base + q * 32 + lane;
-        bool valid = pos < n;
-        key[q] = valid ? keys_in[pos] : 0;
+    for (int q = 0; q < SCAT_ROUNDS; ++q) {
+        const int o = wbase + q * 32 + lane;
+        const bool valid = o < nvalid;
+        key[q] = valid ? kin[o] : 0;
 #pragma unroll
         for (int w = 0; w < W; ++w)
-            pay[w][q] = !valid ? 0 : w == pl.pos_word ? (int32_t)pos : pl.in[w][pos];
+            pay[w][q] = !valid ? 0 : w == pl.pos_word ? (int32_t)(tile0 + o) : pl.in[w][tile0 + o];
+    }
+#pragma unroll
+    for (int q = 0; q < SCAT_ROUNDS; ++q) {
+        const bool valid = wbase + q * 32 + lane < nvalid;
         // invalid lanes get a private digit so they never match a real one
-        int d = valid ? ((key[q] >> shift) & (RADIX_BINS - 1)) : (RADIX_BINS + lane);
-        unsigned peers = __match_any_sync(0xffffffffu, d);
-        int before = valid ? wcnt[warp][d] : 0;
+        const int d = valid ? ((key[q] >> shift) & (RADIX_BINS - 1)) : (RADIX_BINS + lane);
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int before = valid ? wcnt[warp][d] : 0;
         rank[q] = valid ? before + __popc(peers & lt_mask) : -1;
         __syncwarp();
         if (valid && (__ffs(peers) - 1) == lane) wcnt[warp][d] = before + __popc(peers);
         __syncwarp();
     }
     __syncthreads();
-    int cnt = 0;  // keys of digit threadIdx.x in this tile
-    for (int w = 0; w < RADIX_WARPS; ++w) {  // exclusive prefix over warps for digit threadIdx.x
-        const int t = wcnt[w][threadIdx.x];
-        wcnt[w][threadIdx.x] = cnt;
-        cnt += t;
-    }
-    {   // tstart = exclusive scan of cnt over the 256 digits
-        int v = cnt;
+    int cnt = 0, incl = 0;  // keys of digit threadIdx.x in this tile; inclusive scan over digits
+    if (digit_thread) {
+        for (int w = 0; w < SCAT_WARPS; ++w) {  // exclusive prefix over warps for this digit
+            const int t = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = cnt;
+            cnt += t;
+        }
+        incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += u;
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        if (lane == 31) wsum[warp] = v;
-        __syncthreads();
+        if (lane == 31) wsum[warp] = incl;
+    }
+    __syncthreads();
+    if (digit_thread) {  // tstart = exclusive scan of cnt over the 256 digits
         int add = 0;
         for (int w = 0; w < warp; ++w) add += wsum[w];
-        tstart[threadIdx.x] = add + v - cnt;
+        const int ts = add + incl - cnt;
+        tstart[threadIdx.x] = ts;
+        goff[threadIdx.x] -= ts;  // a sorted slot j of digit d goes to goff[d] + j
     }
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < RADIX_ROUNDS; ++q) {
+    for (int q = 0; q < SCAT_ROUNDS; ++q) {
         if (rank[q] < 0) continue;
         const int d = (key[q] >> shift) & (RADIX_BINS - 1);
         const int lp = tstart[d] + wcnt[warp][d] + rank[q];
@@ -228,30 +247,28 @@ radix_scatter_kernel(const int32_t *__restrict__ keys_in, int32_t *__restrict__ 
         for (int w = 0; w < W; ++w) spay[w * RADIX_TILE + lp] = pay[w][q];
     }
     __syncthreads();
-    const int nvalid = (int)(n - tile0 < RADIX_TILE ? n - tile0 : RADIX_TILE);
-    for (int j = threadIdx.x; j < nvalid; j += RADIX_THREADS) {
+#pragma unroll 2
+    for (int j = threadIdx.x; j < nvalid; j += SCAT_THREADS) {
         const int32_t k = skey[j];
         const int d = (k >> shift) & (RADIX_BINS - 1);
-        const int64_t dst = (int64_t)goff[d] + (j - tstart[d]);
+        const int dst = goff[d] + j;
         keys_out[dst] = k;
 #pragma unroll
         for (int w = 0; w < W; ++w) pl.out[w][dst] = spay[w * RADIX_TILE + j];
     }
 }
 
-// One scatter pass: the launch with its dynamic shared memory ((1 + W) 16 KB tiles; above the
-// default 48 KB per CTA for W >= 2, so the limit is raised first).
+// One scatter pass: the launch with its dynamic shared memory ((1 + W) 16 KB tiles; the limit
+// is raised first, as the static counters and the dynamic tiles together pass 48 KB).
 template <int W>
 cudaError_t launch_scatter(const int32_t *keys_in, int32_t *keys_out, const Payload &pl, int64_t n,
                            int shift, int64_t ntiles, const int32_t *hist, cudaStream_t st) {
     const size_t dyn = sizeof(int32_t) * (size_t)(1 + W) * RADIX_TILE;
-    if (W >= 2) {
-        cudaError_t e = cudaFuncSetAttribute(radix_scatter_kernel<W>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-        if (e != cudaSuccess) return e;
-    }
-    radix_scatter_kernel<W><<<(unsigned)ntiles, RADIX_THREADS, dyn, st>>>(keys_in, keys_out, pl, n,
-                                                                        shift, ntiles, hist);
+    cudaError_t e = cudaFuncSetAttribute(radix_scatter_kernel<W>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    radix_scatter_kernel<W><<<(unsigned)ntiles, SCAT_THREADS, dyn, st>>>(keys_in, keys_out, pl, n,
+                                                                       shift, ntiles, hist);
     return cudaGetLastError();
 }
 
@@ -400,16 +417,24 @@ cudaError_t radix_sort_pairs(const int32_t *keys_in, const int32_t *vals_in, int
     return cudaGetLastError();
 }
 
+// Key + payload sets a payload-carrying sort of `cols` column ids passes through: the first pass
+// reads the inputs and the last writes the outputs, so one pass needs none, two passes one (the
+// 17,770 columns of the Netflix shape), more passes two in turn.
+static int transpose_sets(int64_t cols) {
+    const int passes = radix_passes((int32_t)(cols > 0 ? cols - 1 : 0));
+    return passes >= 3 ? 2 : passes - 1;
+}
+
 size_t transpose_scratch_bytes(int64_t rows, int64_t cols, int64_t nnz, bool compact) {
     (void)rows;
-    (void)cols;
     const size_t arr = align256(sizeof(int32_t) * (size_t)(nnz > 0 ? nnz : 1));
     if (compact) return 3 * arr + radix_sort_scratch_bytes(nnz);
-    // rows of the CSR, the sorted keys, two ping-pong sets of key + three payload words, the
+    // rows of the CSR, the sorted keys, the ping-pong sets of key + three payload words, the
     // per-tile digit histogram and its scan
     const int64_t ntiles = ceil_div(nnz > 0 ? nnz : 1, RADIX_TILE);
     const size_t hist = (size_t)RADIX_BINS * (size_t)ntiles;
-    return 10 * arr + align256(sizeof(int32_t) * hist) + scan_scratch_bytes((int64_t)hist);
+    return (2 + 4 * (size_t)transpose_sets(cols)) * arr + align256(sizeof(int32_t) * hist) +
+           scan_scratch_bytes((int64_t)hist);
 }
 
 cudaError_t expand_rows(int64_t rows, int64_t nnz, const int32_t *ptr, int32_t *coo_rows,
@@ -444,12 +469,14 @@ cudaError_t csr_to_csc_device(int64_t rows, int64_t cols, int64_t nnz, const int
     } else {
         // sort the columns with the rating's row and value (and its CSR position when the caller
         // keeps the permutation) as payload: the last pass writes the CSC arrays themselves
-        int32_t *set[2][4];
-        for (int k = 0; k < 2; ++k)
+        const int nsets = transpose_sets(cols);
+        int32_t *set[2][4] = {};
+        for (int k = 0; k < nsets; ++k)
             for (int w = 0; w < 4; ++w) set[k][w] = (int32_t *)(s + (2 + 4 * k + w) * arr);
         const int64_t ntiles = ceil_div(nnz, RADIX_TILE);
-        int32_t *hist = (int32_t *)(s + 10 * arr);
-        void *scan_scratch = s + 10 * arr + align256(sizeof(int32_t) * (size_t)RADIX_BINS * ntiles);
+        char *hs = s + (2 + 4 * (size_t)nsets) * arr;
+        int32_t *hist = (int32_t *)hs;
+        void *scan_scratch = hs + align256(sizeof(int32_t) * (size_t)RADIX_BINS * ntiles);
         const int passes = radix_passes((int32_t)(cols > 0 ? cols - 1 : 0));
         for (int pass = 0; pass < passes; ++pass) {
             const bool last = pass == passes - 1;
