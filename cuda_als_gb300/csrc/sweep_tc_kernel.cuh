@@ -18,9 +18,12 @@ namespace tcg {
 
 constexpr int KC = 64;                       // ratings per stage
 constexpr int MAX_NSTAGE = 16;
-// CG at FP = 112 quad-blocks its rows (cg_quad): half of a row's values in registers, half in
-// shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups fit an SM.
-__host__ __device__ constexpr bool cg_quad_rows(int solver, int fp) { return solver == 0 && fp == 112; }
+// CG at FP = 112 and 128 quad-blocks its rows (cg_quad): half of a row's values in registers,
+// half in shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups (FP = 112)
+// or three (FP = 128, as many as its accumulators) fit an SM.
+__host__ __device__ constexpr bool cg_quad_rows(int solver, int fp) {
+    return solver == 0 && (fp == 112 || fp == 128);
+}
 __host__ __device__ constexpr int cgq_floats(int fp) { return 2 * (fp / 16) * 130 * 4; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B
 constexpr int ATOM_STRIDE = (KC / 8) * ATOM_BYTES;  // 8192: LBO between 64-feature atoms
@@ -53,16 +56,23 @@ constexpr int NSOLVER = 4;
 // columns 0 and 1 hold p's high and low f16 parts, the others stay zero.
 __host__ __device__ constexpr int cgtc_tile_floats(int fp) { return (fp / 8) * 64 + 64; }
 
-// TMEM accumulators (ng + 16 columns: two fit in 256 columns unless FP = 128, whose rows have
-// ng = 128) and solver groups: CG and LU read their row out of TMEM into registers at once and
-// release the buffer, so the MMA fills the next row while they solve; their register-resident
-// rows allow two groups per SM.  A Cholesky group keeps its buffer until refinement has re-read
-// A, and its factor lives in shared memory: one group per buffer; so does the quad-blocked CG
-// (half of each row in shared memory), and the tensor-core CG, whose products read A from the
-// buffer until the solve ends.
-__host__ __device__ constexpr int nbuf_of(int fp) { return fp == 128 ? 2 : 4; }
+// TMEM accumulators (ng + 16 columns: four fit in 512 columns unless FP = 128, whose rows have
+// ng = 128: two at a 256-column stride, or three at 160 for the quad-blocked CG, whose stride
+// need not be a power of two) and solver groups: CG and LU read their row out of TMEM into
+// registers at once and release the buffer, so the MMA fills the next row while they solve;
+// their register-resident rows allow two groups per SM.  A Cholesky group keeps its buffer until
+// refinement has re-read A, and its factor lives in shared memory: one group per buffer; so does
+// the quad-blocked CG (half of each row in shared memory), and the tensor-core CG, whose products
+// read A from the buffer until the solve ends.
+__host__ __device__ constexpr int nbuf_of(int solver, int fp) {
+    return fp != 128 ? 4 : cg_quad_rows(solver, fp) ? 3 : 2;
+}
+__host__ __device__ constexpr int acc_stride_of(int solver, int fp, int ng) {
+    return ng + 16 <= 128 ? 128 : nbuf_of(solver, fp) == 3 ? 160 : 256;
+}
 __host__ __device__ constexpr int nepi_of(int solver, int fp) {
-    return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(fp) : nbuf_of(fp) / 2;
+    return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(solver, fp)
+                                                                   : nbuf_of(solver, fp) / 2;
 }
 // Gather warps: as many as the registers the solvers need allow.  A launch's registers are
 // shared out per four warps, so above 640 threads a thread keeps 80 and at 640 it keeps 96: the
@@ -175,13 +185,15 @@ inline Geometry geometry(int f, int solver, bool f8 = false) {
     g.fp = fp_of(f);
     g.fst = (f + 7) / 8 * 8;
     g.ng = (f + 15) / 16 * 16;
-    const int acc_cols = g.ng + 16;
-    g.acc_stride = acc_cols <= 128 ? 128 : 256;
+    g.acc_stride = acc_stride_of(solver, g.fp, g.ng);
     // Accumulators rotate over the groups (group g takes rows g, g + nepi, ...; row k lands in
-    // buffer k % nbuf); nbuf_of(FP) agrees with acc_cols for every f of that padded size.
-    g.nbuf = nbuf_of(g.fp);
+    // buffer k % nbuf); nbuf_of agrees with ng + 16 for every f of that padded size.
+    g.nbuf = nbuf_of(solver, g.fp);
     g.nepi = nepi_of(solver, g.fp);
-    g.tmem_cols = g.nbuf * g.acc_stride;
+    // the allocation is a power of two of at least 32 columns (three 160-column buffers: 512)
+    int cols = 32;
+    while (cols < g.nbuf * g.acc_stride) cols *= 2;
+    g.tmem_cols = cols;
     g.nthreads = nthreads_of(solver, g.fp);
     const int ns = nstage_of(solver, g.fp, f8);
     size_t bytes = (size_t)ns * stage_bytes(f8);                     // operand ring
