@@ -258,16 +258,18 @@ struct TriLayout {
 // Cholesky A = L L^T of the padded FP x FP matrix held in Ls (packed, tri_off rows; entry (i, j)
 // for j <= i must be set, the rest of each row's blocks is scratch).  On exit entry (i, j <= i)
 // holds L[i][j], Dv[K * 64 + r * 8 + c] = (L_KK^-1)[r][c] for r >= c (the inverse of each 8 x 8
-// diagonal block) and invd[j] = 1 / L[j][j].  Called by the 128 threads of a group (et = 0..127).
+// diagonal block) and invd[j] = 1 / L[j][j].  Called by the 128 threads of a group (et = 0..127);
+// thread `lead` factors the diagonal blocks.
 //
 // Left-looking in blocks of 8 columns, three barriers per block:
 //  (a) every (row r >= k0, half h) pair subtracts L[r][0:k0] . L[k0+4h+kk][0:k0], kk < 4, from
 //      its 4 entries: work spread evenly over the 128 threads whatever the row count left;
-//  (b) one thread factors the 8 x 8 diagonal block in registers (rsqrt pivots) and inverts it;
+//  (b) one thread (lead) factors the 8 x 8 diagonal block in registers (rsqrt pivots) and
+//      inverts it;
 //  (c) every row below takes its block columns as s L_KK^-T.
-// Returns false (on thread 0) if a pivot was not positive and finite.
+// Returns false (on thread lead) if a pivot was not positive and finite.
 template <int FP>
-__device__ bool chol_fac(int et, float *Ls, float *Dv, float *invd, const GroupSync &gs) {
+__device__ bool chol_fac(int et, int lead, float *Ls, float *Dv, float *invd, const GroupSync &gs) {
     constexpr int B = 8;
     bool ok = true;
 #pragma unroll 1
@@ -304,7 +306,7 @@ __device__ bool chol_fac(int et, float *Ls, float *Dv, float *invd, const GroupS
             }
             gs.sync();
         }
-        if (et == 0) {
+        if (et == lead) {
             // (b) factor: right-looking inside the block, everything in registers
             float m[B][B];
 #pragma unroll

@@ -512,6 +512,11 @@ __device__ __forceinline__ double tmem_rowdot(uint32_t tb, int ng, const float *
     return WIDE ? acc : (double)accf;
 }
 
+// A group's serial work (the waits on its barriers, the tensor-core CG's MMA chains, the
+// Cholesky factor's diagonal blocks and triangular solves) runs on warp g % 4 of group g: warps
+// are spread over the SM's four sub-partitions by warp index % 4, so the groups' leaders sit on
+// four different schedulers instead of all on the first.
+__device__ __forceinline__ int lead_of(int g) { return 32 * (g & 3); }
 __device__ __forceinline__ int lane_of(int i) { return i & 31; }
 
 // The tensor-core CG's per-group state that outlives a row: the phase of its product barrier, and
@@ -533,12 +538,12 @@ struct CgTcState {
 // A [hi lo] to columns [ng, ng + 16) (b was read from there before), and thread i sums its two
 // values and undoes both scales (powers of two: exact).  The scaling keeps binary16's 11-bit
 // rounding but not its exponent range: no entry overflows or loses bits to subnormals.  The
-// group's leader (et == 0) issues the chain and commits it to `bar`; every warp waits on the
+// group's leader (et == lead) issues the chain and commits it to `bar`; every warp waits on the
 // barrier itself.  Thread i holds x_i, r_i, p_i; padded rows (i >= f) keep zeros.
 template <int FP>
 __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, float xi, int i,
-                       int et, __half *Bh, int ka, uint32_t bar, CgTcState &st, float *red,
-                       volatile int *abort, const GroupSync &gs, bool &ok) {
+                       int et, int lead, __half *Bh, int ka, uint32_t bar, CgTcState &st,
+                       float *red, volatile int *abort, const GroupSync &gs, bool &ok) {
     int slot = 0;
     const int ng = p.ng;
     const uint32_t idesc = idesc_f16(128, 16);
@@ -554,7 +559,7 @@ __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, 
         fence_async_smem();  // the tile is read by the tensor core (async proxy)
         tc_fence_before();   // the previous product's tcgen05.ld precede the next MMA
         gs.sync();
-        if (et == 0 && !*abort) {
+        if (et == lead && !*abort) {
             tc_fence_after();
             for (int kk = 0; kk < ng / 16; ++kk)
                 mma_f16_tmem_a(tcol + (uint32_t)ng, tcol + 8u * kk,
@@ -565,7 +570,7 @@ __device__ float cg_tc(const Params &p, uint32_t tcol, uint32_t trow, float bi, 
         }
         const bool done = mbar_wait_warp(bar, st.phase & 1, abort, p.wait_ns);
         if (done) {
-            if (et == 0) st.unconfirmed = false;
+            if (et == lead) st.unconfirmed = false;
         } else {
             ok = false;
             if ((threadIdx.x & 31) == 0) *abort = 1;
@@ -675,11 +680,11 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         if (i < FP) yv[i] = bi;
         if (et == 0) cflag[0] = 0;
         gs.sync();
-        if (!chol_fac<FP>(et, Ls, Dv, invd, gs)) cflag[0] = 1;
+        if (!chol_fac<FP>(et, lead_of(g), Ls, Dv, invd, gs)) cflag[0] = 1;
         gs.sync();
         good = cflag[0] == 0;
         if (good) {
-            if (wg == 0) {
+            if (wg == (g & 3)) {
                 chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
                 // condition estimate from the Cholesky diagonal: (max L_jj / min L_jj)^2
                 float dmax = 0.f, dmin = 3.0e38f;
@@ -693,7 +698,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
                     dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
                 }
-                if (i == 0) cflag[1] = (dmax / dmin) * (dmax / dmin) > p.cond_threshold ? 1 : 0;
+                if (i == lead_of(g))
+                    cflag[1] = (dmax / dmin) * (dmax / dmin) > p.cond_threshold ? 1 : 0;
             }
             gs.sync();
             xi = i < f ? yv[i] : 0.f;
@@ -710,7 +716,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     ri = bi - (float)ax - reg * xi;
                 if (i < FP) yv[i] = i < f ? ri : 0.f;
                 gs.sync();
-                if (wg == 0) chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
+                if (wg == (g & 3)) chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
                 gs.sync();
                 if (i < f) xi += yv[i];
             }
@@ -764,7 +770,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             }
         }
         tmem_wait_st();
-        xi = cg_tc<FP>(p, tb & 0xFFFFu, tb, bi, i < f ? xw : 0.f, i, et,
+        xi = cg_tc<FP>(p, tb & 0xFFFFu, tb, bi, i < f ? xw : 0.f, i, et, lead_of(g),
                        reinterpret_cast<__half *>(Ls), ka, mvbar, cst, red, abort, gs, ok);
     } else {
         // CG / LU work on the row in registers: a[j] = A[i][j] (+ lambda n_u on the diagonal)
@@ -1218,7 +1224,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         bool ok = true;
         CgTcState cst;
         auto group_wait = [&](uint32_t bar, uint32_t parity) -> bool {
-            if (et == 0) *okflag = mbar_wait(bar, parity, abort, p.wait_ns) ? 1 : 0;
+            if (et == lead_of(g)) *okflag = mbar_wait(bar, parity, abort, p.wait_ns) ? 1 : 0;
             gs.sync();
             const bool r = *okflag != 0;
             gs.sync();
@@ -1254,7 +1260,7 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
         // a product chain whose completion was not seen (a wait ran out) finishes before TMEM is
         // released: after a failed wait the leader issues nothing more, so it is the last one
         // (product calls after the abort commit nothing: wait for the last commit's phase)
-        if (SOLVER == SOLVER_CGTC && et == 0 && cst.unconfirmed)
+        if (SOLVER == SOLVER_CGTC && et == lead_of(g) && cst.unconfirmed)
             mbar_wait(smem_u32(&mvbar[g]), cst.committed & 1, nullptr, WAIT_NS);
         if (!ok) {  // (the tensor-core CG's waits are per warp: each failing warp counts)
             *abort = 1;
