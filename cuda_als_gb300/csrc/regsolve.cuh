@@ -131,34 +131,6 @@ __device__ float cg_reg(const float (&a)[FP], float bi, float xi, int i, float *
     return cg_single_reduction(mul, bi, xi, red, iters, tol, gs);
 }
 
-template <int FP>
-__device__ float cg_reg_two_reductions(const float (&a)[FP], float bi, float xi, int i, float *sv,
-                                       float *red, int iters, float tol, const GroupSync &gs) {
-    int slot = 0;
-    const bool live = i < FP;  // threads past the padded size hold zero rows and write nothing
-    if (live) sv[i] = xi;
-    gs.sync();
-    float r = bi - dot_row<FP>(a, sv);
-    float p = r;
-    float rsold = gsum128(r * r, red, slot, gs);
-    for (int it = 0; it < iters; ++it) {
-        if (live) sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
-        gs.sync();
-        const float ap = dot_row<FP>(a, sv);
-        const float pap = gsum128(p * ap, red, slot, gs);
-        if (!(pap > 0.f)) break;
-        const float alpha = rsold / pap;
-        xi = fmaf(alpha, p, xi);
-        r = fmaf(-alpha, ap, r);
-        const float rsnew = gsum128(r * r, red, slot, gs);
-        if (rsnew < tol) break;
-        const float beta = rsnew / rsold;
-        rsold = rsnew;
-        p = fmaf(beta, p, r);
-    }
-    return xi;
-}
-
 // CG as cg_reg with the rows quad-blocked (FP = 112).  The four lanes 4a..4a+3 of a warp share
 // rows 4a..4a+3: lane 4a+c holds columns 16k+4c..16k+4c+3 (k < NK = FP/16) of all four, rows 4a
 // and 4a+1 in registers (ar[0], ar[1]), rows 4a+2 and 4a+3 in shared memory (slots 2k and 2k+1
@@ -199,47 +171,20 @@ __device__ __forceinline__ float dot_quad(const float4 (&ar)[2][NK], const float
     return (odd ? k1 : k0) + __shfl_xor_sync(0xffffffffu, odd ? k0 : k1, 1);
 }
 
+// The quad-blocked rows hold the Gram without its diagonal term: thread i adds dreg * v_i (lambda
+// n_u, or 1 on a padded row, whose Gram row is zero) to each product.
 template <int NK>
 __device__ float cg_quad(const float4 (&ar)[2][NK], const float4 *sa, float bi, float xi, int i,
-                         float *sv, float *red, int iters, float tol, const GroupSync &gs) {
+                         float *sv, float *red, int iters, float tol, const GroupSync &gs,
+                         float dreg) {
     constexpr int FP = 16 * NK;
     const bool live = i < FP;
     auto mul = [&](float v) -> float {
         if (live) sv[i] = v;
         gs.sync();
-        return dot_quad<NK>(ar, sa, sv, i);
+        return fmaf(dreg, v, dot_quad<NK>(ar, sa, sv, i));
     };
     return cg_single_reduction(mul, bi, xi, red, iters, tol, gs);
-}
-
-template <int NK>
-__device__ float cg_quad_two_reductions(const float4 (&ar)[2][NK], const float4 *sa, float bi,
-                                        float xi, int i, float *sv, float *red, int iters,
-                                        float tol, const GroupSync &gs) {
-    constexpr int FP = 16 * NK;
-    int slot = 0;
-    const bool live = i < FP;
-    if (live) sv[i] = xi;
-    gs.sync();
-    float r = bi - dot_quad<NK>(ar, sa, sv, i);
-    float p = r;
-    float rsold = gsum128(r * r, red, slot, gs);
-    for (int it = 0; it < iters; ++it) {
-        if (live) sv[i] = p;  // every thread finished reading sv in the previous gsum's barrier
-        gs.sync();
-        const float ap = dot_quad<NK>(ar, sa, sv, i);
-        const float pap = gsum128(p * ap, red, slot, gs);
-        if (!(pap > 0.f)) break;
-        const float alpha = rsold / pap;
-        xi = fmaf(alpha, p, xi);
-        r = fmaf(-alpha, ap, r);
-        const float rsnew = gsum128(r * r, red, slot, gs);
-        if (rsnew < tol) break;
-        const float beta = rsnew / rsold;
-        rsold = rsnew;
-        p = fmaf(beta, p, r);
-    }
-    return xi;
 }
 
 // Packed lower triangle of an FP x FP factor in shared memory.  Row i (block K = i / 8) keeps

@@ -791,6 +791,10 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                 tmem_ld2(tb + p.ng, b0, b1);
                 bi = i < f ? b0 * di : 0.f;
             }
+            // The accumulator's columns f..ng-1 are zero (the table's padded features are zero
+            // and the gathers fill zeros past them), so only a chunk reaching column ng (b) is
+            // cut there; rows i >= f are cleared; the diagonal term (lambda n_u, 1 on the padded
+            // rows) is added in every product instead (cg_quad).
 #pragma unroll
             for (int k = 0; k < NK; ++k) {
                 float v[16];
@@ -800,16 +804,16 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
 #pragma unroll
                         for (int j = 0; j < 16; ++j) v[j] *= di * dsc[16 * k + j];
                     }
+                    if (16 * k + 16 > p.ng) {  // warp-uniform: the chunk holding column ng
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (16 * k + j >= p.ng) v[j] = 0.f;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = i < f ? v[j] : 0.f;
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[j] = 0.f;
-                }
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int col = 16 * k + j;
-                    float x = col < p.ng && i < f ? v[j] : 0.f;
-                    if (col == i) x = i < f ? x + reg : 1.f;  // identity on the padded rows
-                    v[j] = x;
                 }
                 float4 V[4];
 #pragma unroll
@@ -831,7 +835,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
             gs.sync();  // (also orders the slots' stores before the first product)
             if (et == 0) mbar_arrive(release);
             released = true;
-            xi = cg_quad<NK>(ar, sa, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs);
+            xi = cg_quad<NK>(ar, sa, bi, xw, i, sv, red, p.cg_iters, p.cg_tol, gs,
+                             i < f ? reg : 1.f);
         } else {
         // the Gram row (columns < ng) and b (column ng) in one or two TMEM round trips
         float a[FP];
