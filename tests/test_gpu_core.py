@@ -49,7 +49,8 @@ def test_gpu_transpose_matches_reference_prep_logs(toy):
     assert np.array_equal(cval, toy["R_train_csc_data"].astype(np.float32))
 
 
-@pytest.mark.parametrize("case", ["cfg1", "cfg3", "cfg4", "wide", "empty", "one_row", "nnz0"])
+@pytest.mark.parametrize("case", ["cfg1", "cfg3", "cfg4", "wide", "narrow", "empty", "one_row",
+                                  "nnz0"])
 def test_gpu_transpose_bit_exact(case):
     rng = np.random.default_rng(1)
     if case.startswith("cfg"):
@@ -60,6 +61,9 @@ def test_gpu_transpose_bit_exact(case):
     elif case == "wide":   # > 2^16 columns: three radix passes
         m, n = 300, 150000
         ptr, idx, val = random_csr(rng, m, n, density=0.002, values=(0, 9))
+    elif case == "narrow":  # <= 256 columns: one radix pass straight into the CSC arrays
+        m, n = 3000, 200
+        ptr, idx, val = random_csr(rng, m, n, density=0.05)
     elif case == "empty":  # empty rows and empty columns
         m, n = 200, 700
         ptr, idx, val = random_csr(rng, m, n, density=0.01, empty_rows=set(range(0, 200, 3)))
