@@ -14,7 +14,7 @@
 //                 memory, left-looking in blocks of 8 columns: the dot products are spread over
 //                 all 128 threads as (row, column-half) items, one thread factors and inverts
 //                 each 8 x 8 diagonal block in registers, three barriers per block.
-//   chol_solve_warp  L y = b and L^T x = y by one warp with shuffles and no barrier.
+//   chol_solve_group  L y = b and L^T x = y by the group, one barrier per 8-row block.
 // Sums over threads are combined in a fixed order (deterministic).
 #pragma once
 
@@ -333,108 +333,93 @@ __device__ bool chol_fac(int et, int lead, float *Ls, float *Dv, float *invd, co
     return ok;
 }
 
-// x = (L L^T)^-1 v for the factor left by chol_fac, run by ONE warp (lane = its lane) with no
-// barrier: lane l keeps the running values of rows l, l + 32, l + 64, l + 96 in registers.  Each
-// 8-row block is a shuffle of its rows' values, a product with the block inverse (every lane
-// computes all 8 results, so nothing is broadcast), and an update of the rows after it (forward)
-// or before it (backward).  v (FP floats of shared memory) holds b on entry and x on exit.
+// x = (L L^T)^-1 v for the factor left by chol_fac, by the whole group: thread t keeps the
+// running value of row t.  Per 8-row block (forward, then backward from the bottom) the warp that
+// owns the block's rows forms its 8 results with the block's inverse (lane l0 + c computes result
+// c from shuffles of the block rows' running values) and publishes them in `xb`; after one barrier
+// every thread folds them into its own row: forward L[t][k0..k0+7] . y, backward
+// L[k0..k0+7][t] . x.  Each row sees the same FMA sequence as in a one-warp solve.  Blocks use the
+// two 8-float halves of `xb` in turn (the backward sweep starting on the half the forward sweep did
+// not end on), so a block's writer never overwrites values a thread has yet to read.  v (FP floats
+// of shared memory) holds b on entry and x on exit, each thread reading and writing its own row.
 template <int FP>
-__device__ __forceinline__ float pick(const float (&v)[(FP + 31) / 32], int j) {
-    float r = v[0];
-#pragma unroll
-    for (int q = 1; q < (FP + 31) / 32; ++q)
-        if (j == q) r = v[q];
-    return r;
-}
-
-template <int FP>
-__device__ void chol_solve_warp(int lane, const float *Ls, const float *Dv, float *v) {
+__device__ void chol_solve_group(int et, const float *Ls, const float *Dv, float *v, float *xb,
+                                 const GroupSync &gs) {
     constexpr int B = 8;
-    constexpr int NJ = (FP + 31) / 32;
-    float acc[NJ];
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-        const int r = lane + 32 * j;
-        acc[j] = r < FP ? v[r] : 0.f;
-    }
-    // forward: L y = b.  The block loops stay rolled (compact code, no hoisted loads); the
-    // running value of the block's rows is picked from acc[] by selects, not by indexing.
+    constexpr int NB = FP / B;
+    const int lane = et & 31, w = et >> 5;
+    const bool live = et < FP;
+    float acc = live ? v[et] : 0.f;
+    // forward: L y = b
 #pragma unroll 1
-    for (int K = 0; K < FP / B; ++K) {
-        const int k0 = K * B, jb = k0 >> 5, l0 = k0 & 31;
-        const float *dv = Dv + K * B * B;
-        const float cur = pick<FP>(acc, jb);
-        float r[B], y[B];
+    for (int K = 0; K < NB; ++K) {
+        const int k0 = K * B;
+        float *yb = xb + (K & 1) * B;
+        if (w == (k0 >> 5)) {  // warp-uniform: the warp holding rows k0..k0+7
+            const int l0 = k0 & 31, c = lane - l0;
+            float r[B];
 #pragma unroll
-        for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, cur, l0 + q);
-        float mine = cur;
+            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, acc, l0 + q);
+            if (c >= 0 && c < B) {
+                const float *dr = Dv + K * B * B + c * B;  // row c of the block's inverse, q <= c
+                float y = 0.f;
 #pragma unroll
-        for (int c = 0; c < B; ++c) {
-            float t = 0.f;
-#pragma unroll
-            for (int q = 0; q <= c; ++q) t = fmaf(dv[c * B + q], r[q], t);
-            y[c] = t;
-            if (lane == l0 + c) mine = t;
+                for (int q = 0; q < B; ++q)
+                    if (q <= c) y = fmaf(dr[q], r[q], y);
+                acc = y;
+                yb[c] = y;
+            }
         }
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int row = lane + 32 * j;
-            if (j == jb) {
-                if (row >= k0 && row < k0 + B) acc[j] = mine;
-            }
-            if (row >= k0 + B && row < FP) {
-                const float4 a0 = *reinterpret_cast<const float4 *>(Ls + tri_off(row) + k0);
-                const float4 a1 = *reinterpret_cast<const float4 *>(Ls + tri_off(row) + k0 + 4);
-                float t = acc[j];
-                t = fmaf(-a0.x, y[0], t);
-                t = fmaf(-a0.y, y[1], t);
-                t = fmaf(-a0.z, y[2], t);
-                t = fmaf(-a0.w, y[3], t);
-                t = fmaf(-a1.x, y[4], t);
-                t = fmaf(-a1.y, y[5], t);
-                t = fmaf(-a1.z, y[6], t);
-                t = fmaf(-a1.w, y[7], t);
-                acc[j] = t;
-            }
+        gs.sync();
+        if (live && et >= k0 + B) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(Ls + tri_off(et) + k0);
+            const float4 a1 = *reinterpret_cast<const float4 *>(Ls + tri_off(et) + k0 + 4);
+            const float4 y0 = *reinterpret_cast<const float4 *>(yb);
+            const float4 y1 = *reinterpret_cast<const float4 *>(yb + 4);
+            float t = acc;
+            t = fmaf(-a0.x, y0.x, t);
+            t = fmaf(-a0.y, y0.y, t);
+            t = fmaf(-a0.z, y0.z, t);
+            t = fmaf(-a0.w, y0.w, t);
+            t = fmaf(-a1.x, y1.x, t);
+            t = fmaf(-a1.y, y1.y, t);
+            t = fmaf(-a1.z, y1.z, t);
+            t = fmaf(-a1.w, y1.w, t);
+            acc = t;
         }
     }
     // backward: L^T x = y, blocks from the bottom
 #pragma unroll 1
-    for (int K = FP / B - 1; K >= 0; --K) {
-        const int k0 = K * B, jb = k0 >> 5, l0 = k0 & 31;
-        const float *dv = Dv + K * B * B;
-        const float cur = pick<FP>(acc, jb);
-        float r[B], x[B];
+    for (int K = NB - 1; K >= 0; --K) {
+        const int k0 = K * B;
+        float *xk = xb + ((K + 1) & 1) * B;
+        if (w == (k0 >> 5)) {
+            const int l0 = k0 & 31, c = lane - l0;
+            float r[B];
 #pragma unroll
-        for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, cur, l0 + q);
-        float mine = cur;
+            for (int q = 0; q < B; ++q) r[q] = __shfl_sync(0xffffffffu, acc, l0 + q);
+            if (c >= 0 && c < B) {
+                const float *dc = Dv + K * B * B + c;  // column c of the block's inverse, q >= c
+                float x = 0.f;
 #pragma unroll
-        for (int c = 0; c < B; ++c) {
-            float t = 0.f;
-#pragma unroll
-            for (int q = c; q < B; ++q) t = fmaf(dv[q * B + c], r[q], t);
-            x[c] = t;
-            if (lane == l0 + c) mine = t;
-        }
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-            const int row = lane + 32 * j;
-            if (j == jb) {
-                if (row >= k0 && row < k0 + B) acc[j] = mine;
-            }
-            if (row < k0) {
-                float t = acc[j];
-#pragma unroll
-                for (int kk = 0; kk < B; ++kk) t = fmaf(-Ls[tri_off(k0 + kk) + row], x[kk], t);
-                acc[j] = t;
+                for (int q = 0; q < B; ++q)
+                    if (q >= c) x = fmaf(dc[q * B], r[q], x);
+                acc = x;
+                xk[c] = x;
             }
         }
-    }
+        gs.sync();
+        if (live && et < k0) {
+            const float4 x0 = *reinterpret_cast<const float4 *>(xk);
+            const float4 x1 = *reinterpret_cast<const float4 *>(xk + 4);
+            const float xs[B] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+            float t = acc;
 #pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-        const int r = lane + 32 * j;
-        if (r < FP) v[r] = acc[j];
+            for (int kk = 0; kk < B; ++kk) t = fmaf(-Ls[tri_off(k0 + kk) + et], xs[kk], t);
+            acc = t;
+        }
     }
+    if (live) v[et] = acc;
 }
 
 }  // namespace als

@@ -639,7 +639,7 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
     if constexpr (SOLVER == SOLVER_CHOL) {
         // Cholesky (+ refinement against the TMEM copy of A).  The regularised Gram's lower
         // triangle moves to the packed shared-memory layout in 32-column chunks (a warp reads
-        // only the chunks its rows reach), the group factors it, one warp runs each pair of
+        // only the chunks its rows reach), the group factors it and runs each pair of
         // triangular solves.
         float *Dv = Ls + TriLayout<FP>::floats;
         float *invd = vec;                                                   // 1 / L_jj
@@ -684,8 +684,9 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
         gs.sync();
         good = cflag[0] == 0;
         if (good) {
+            float *xb = vec + 256;  // the triangular solves' per-block results (16 floats)
+            chol_solve_group<FP>(i, Ls, Dv, yv, xb, gs);
             if (wg == (g & 3)) {
-                chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
                 // condition estimate from the Cholesky diagonal: (max L_jj / min L_jj)^2
                 float dmax = 0.f, dmin = 3.0e38f;
                 for (int j = lane_of(i); j < f; j += 32) {
@@ -714,10 +715,8 @@ __device__ bool solve_row(const Params &p, const Meta &m, uint32_t tb, int i, in
                     ri = (float)((double)bi - ax - (double)reg * (double)xi);
                 else
                     ri = bi - (float)ax - reg * xi;
-                if (i < FP) yv[i] = i < f ? ri : 0.f;
-                gs.sync();
-                if (wg == (g & 3)) chol_solve_warp<FP>(lane_of(i), Ls, Dv, yv);
-                gs.sync();
+                if (i < FP) yv[i] = i < f ? ri : 0.f;  // (the solve reads and writes each
+                chol_solve_group<FP>(i, Ls, Dv, yv, xb, gs);  //  thread's own row)
                 if (i < f) xi += yv[i];
             }
             if (wide && et == 0 && p.refine_steps > 0) atomicAdd(&p.flags[1], 1);
