@@ -18,11 +18,11 @@ namespace tcg {
 
 constexpr int KC = 64;                       // ratings per stage
 constexpr int MAX_NSTAGE = 16;
-// CG at FP = 112 and 128 quad-blocks its rows (cg_quad): half of a row's values in registers,
-// half in shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups (FP = 112)
-// or three (FP = 128, as many as its accumulators) fit an SM.
+// CG at FP = 64, 112 and 128 quad-blocks its rows (cg_quad): half of a row's values in
+// registers, half in shared memory (2 FP/16 slots of CGQ_SLOT float4 a group), so four groups
+// (FP = 64, 112) or three (FP = 128, as many as its accumulators) fit an SM.
 __host__ __device__ constexpr bool cg_quad_rows(int solver, int fp) {
-    return solver == 0 && (fp == 112 || fp == 128);
+    return solver == 0 && fp >= 64;
 }
 __host__ __device__ constexpr int cgq_floats(int fp) { return 2 * (fp / 16) * 130 * 4; }
 constexpr int ATOM_BYTES = 1024;             // 8 ratings x 128 B

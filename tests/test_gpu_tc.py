@@ -86,7 +86,9 @@ def test_tc_half_sweep_matches_oracle_on_bf16_inputs(f):
     assert np.linalg.norm(U - Uf) / np.linalg.norm(Uf) < 2e-2
 
 
-@pytest.mark.parametrize("solve,f", [(ca.SOLVE_TYPE.LU, 100), (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 70),
+@pytest.mark.parametrize("solve,f", [(ca.SOLVE_TYPE.LU, 100), (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 40),
+                                     (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 64),
+                                     (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 70),
                                      (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 90),
                                      (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 100),
                                      (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 112),
@@ -95,9 +97,10 @@ def test_tc_half_sweep_matches_oracle_on_bf16_inputs(f):
                                      (ca.SOLVE_TYPE.CUMF_ALS_CG_FP32, 128),
                                      (ca.SOLVE_TYPE.LU, 128)])
 def test_tc_other_solvers(solve, f):
-    """LU and the FP32 CG on the tensor-core path against the oracle.  f = 70, 90, 100, 112 all
-    pad to 112 (the quad-blocked CG, four groups), with 80, 96 and 112 Gram columns; f = 113,
-    120, 128 pad to 128 (quad-blocked, three groups on 160-column accumulators)."""
+    """LU and the FP32 CG on the tensor-core path against the oracle.  f = 40, 64 pad to 64 and
+    f = 70, 90, 100, 112 to 112 (the quad-blocked CG, four groups), with 48 / 64 and 80 / 96 / 112
+    Gram columns; f = 113, 120, 128 pad to 128 (quad-blocked, three groups on 160-column
+    accumulators)."""
     rng, m, n, ptr, idx, val = stage_boundary_problem(f, seed=7)
     U0 = (rng.standard_normal((m, f)) * 0.1).astype(np.float32)
     V0 = (rng.standard_normal((n, f)) * 0.3).astype(np.float32)
