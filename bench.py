@@ -504,6 +504,18 @@ def run_ours(args):
         fms, fp32 = compare(ca.PRECISION.FP32, ca.SOLVE_TYPE.CHOLESKY)
         fp32.update(solve="cholesky", speedup=round(fms / ms, 3),
                     rmse_delta=abs(rmse - fp32["test_rmse_after_iters"]))
+        # its own roofline: Gram + right-hand-side flops of an epoch on the FP32 CUDA cores,
+        # against their nominal peak at the clock sampled in the timed region
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0
+        ep_flops = 2 * (nnz * f * (f + 1) + 2 * nnz * f)
+        fp32_tf = ep_flops / (fms * 1e-3) / 1e12
+        fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12 if mhz else None
+        fp32.update(gram_rhs_tflops=round(fp32_tf, 3),
+                    fp32_peak_tflops=round(fp32_peak, 1) if fp32_peak else None,
+                    frac_of_fp32_peak=round(fp32_tf / fp32_peak, 4) if fp32_peak else None,
+                    fp32_peak_source="nominal: SMs x 128 FP32 lanes x 2 flops x the sampled SM "
+                                     "clock (no measured FP32 peak)")
         if solve != ca.SOLVE_TYPE.CHOLESKY:
             cms, chol = compare(prec, ca.SOLVE_TYPE.CHOLESKY)
             chol.update(refine_steps=1, speedup_vs_fp32=round(fms / cms, 3),
