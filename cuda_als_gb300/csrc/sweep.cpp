@@ -370,9 +370,17 @@ als_status run_half_sweep(als_handle *h, int side) {
         als_status s = tune_side(h, side, &launches);
         if (s != ALS_OK) return s;
     } else {
-        for (size_t k = 0; k < h->plan[side].size(); ++k)
-            S_CUDA(h, launch_bucket(h, side, h->plan[side][k], h->plan[side][k].solver, (int)k,
-                                    &launches));
+        // adjacent buckets that settled on the same solver are contiguous ranges of the order:
+        // one launch covers them (no tail between them, one launch fewer)
+        const auto &plan = h->plan[side];
+        for (size_t k = 0; k < plan.size();) {
+            size_t last = k;
+            while (last + 1 < plan.size() && plan[last + 1].solver == plan[k].solver) ++last;
+            SweepBucket run = plan[k];
+            run.hi = plan[last].hi;
+            S_CUDA(h, launch_bucket(h, side, run, run.solver, (int)k, &launches));
+            k = last + 1;
+        }
     }
     S_CUDA(h, record_event(h->ev_half[side][1], st));
     h->counters[0] = launches;
