@@ -545,12 +545,21 @@ def run_ours(args):
         with torch.cuda.stream(stream):
             e0.record(stream)
         e2e_rmse = None
+        phase = {"reload": 0.0, "init_and_epochs": 0.0, "readback_and_rmse": 0.0}
         for _ in range(args.steps):
+            # (every call returns once its work is done: host time per phase)
+            ta = time.perf_counter()
             model.reload(tr, te)     # H2D: CSR + test COO, GPU transpose, degree orders
-            model.init_factors()     # srand(0) on the host, V uploaded
+            tb = time.perf_counter()
+            model.init_factors()     # srand(0) on the GPU
             model.iterate(iters)
+            tc = time.perf_counter()
             model.get_factors(U, V)  # D2H: both factor tables
             e2e_rmse = model.rsme_test()
+            td = time.perf_counter()
+            phase["reload"] += tb - ta
+            phase["init_and_epochs"] += tc - tb
+            phase["readback_and_rmse"] += td - tc
         with torch.cuda.stream(stream):
             e1.record(stream)
         barrier()
@@ -561,6 +570,7 @@ def run_ours(args):
         e2e = {"value": round(max(ev, wall), 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "device_event_ms": round(ev, 3),
                "host_wall_ms": round(wall, 3), "test_rmse": e2e_rmse,
+               "phases_ms_per_step": {k: round(v * 1e3 / args.steps, 3) for k, v in phase.items()},
                "step": f"als_reload + als_init_factors + {iters} epochs + both factor tables "
                        f"read back + test RMSE; value per epoch"}
 
