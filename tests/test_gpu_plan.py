@@ -82,6 +82,23 @@ def test_fixed_solver_is_one_bucket():
             assert all(t["ms_cg"] < 0 for t in mdl.tuning(side))
 
 
+def test_auto_plan_launches_one_kernel_per_solver_run():
+    """Adjacent buckets that settled on the same solver are contiguous rows of the order and share
+    one launch: an epoch's kernel count is one BF16 quantise per side plus one launch per run of
+    equal solvers in each side's plan."""
+    tr, te, info = workload2()
+    with model(tr, te, info, ca.SOLVE_TYPE.AUTO, ca.PRECISION.BF16, iters=3) as mdl:
+        mdl.init_factors()
+        mdl.iterate(3)  # the tuning sweeps are over: the plan is final
+        mdl.iterate(1)
+        expected = 0
+        for side in (0, 1):
+            solvers = [b["solver"] for b in mdl.plan(side)]
+            expected += 1 + sum(1 for k in range(len(solvers))
+                                if k == 0 or solvers[k] != solvers[k - 1])
+        assert mdl.counters()["launches"] == expected
+
+
 @pytest.mark.parametrize("precision", [ca.PRECISION.BF16, ca.PRECISION.FP32])
 def test_auto_training_reaches_fp32_cholesky_rmse(precision):
     """Full-size workload 2 (69,878 x 10,677, 10M ratings, f = 64), 10 iterations.  (Scaled-down
