@@ -86,8 +86,12 @@ als_status refresh_csc_values(als_handle *h) {
 // ---------------------------------------------------------------------------- kernel plan
 
 // Relative agreement the autotuner asks of CG against Cholesky on a bucket's rows (Frobenius norm
-// of the difference over the norm of the Cholesky solution) at the tuning sweep.
-constexpr double AUTO_TOL = 2e-2;
+// of the difference over the norm of the Cholesky solution) at the tuning sweep.  The tuning
+// sweep is the first warm start, where six CG steps are furthest from converged; on rows lighter
+// than f (rank-deficient Grams) they land 2-3e-2 from Cholesky there (MovieLens-latest-shaped
+// items) and keep the test RMSE within 5e-5 of plain FP32 Cholesky after training, as the
+// reference's own configurations run CG on every row.
+constexpr double AUTO_TOL = 5e-2;
 // The tuning sweep runs on the first warm start, where CG takes all its steps; later epochs exit
 // earlier, which favours the solver with the smaller fixed cost per row.  The tensor-core CG pays
 // a scale reduction and a packing pass per row, so it must beat the best other solver by this

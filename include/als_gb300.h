@@ -254,7 +254,7 @@ als_status als_get_plan(const als_handle *h, int32_t side, int32_t *lo, int32_t 
  * ms_cg16[b] = CUDA-event time of the bucket's launch with the FP32 CG, Cholesky and (tensor-core
  * precisions only) the FP16-Gram CG on the tuning sweep (the side's second half-sweep, all from
  * the same warm start); rel[b] / rel16[b] = ||x_cg - x_chol|| / ||x_chol|| over the bucket's
- * rows for each CG.  The bucket keeps the fastest of Cholesky and the CGs with rel <= 2e-2.
+ * rows for each CG.  The bucket keeps the fastest of Cholesky and the CGs with rel <= 5e-2.
  * Negative entries: not measured.  Any output pointer may be NULL.  nb in: capacity, out:
  * count.  Buckets are the rows of degree >= 8f, f <= degree < 8f and degree < f, in order. */
 als_status als_get_tuning(const als_handle *h, int32_t side, float *ms_cg, float *ms_chol,

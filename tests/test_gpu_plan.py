@@ -14,7 +14,7 @@ import cuda_als_gb300 as ca
 
 pytestmark = pytest.mark.gpu
 
-AUTO_TOL = 2e-2             # the tuner's CG-vs-Cholesky agreement bound (sweep.cpp)
+AUTO_TOL = 5e-2             # the tuner's CG-vs-Cholesky agreement bound (sweep.cpp)
 CG16_MARGIN = 0.85          # the lead it asks of the tensor-core CG (sweep.cpp)
 TOL_RMSE = 2e-3          # test RMSE after training vs plain FP32 Cholesky
 
