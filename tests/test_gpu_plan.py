@@ -99,11 +99,14 @@ def test_auto_plan_launches_one_kernel_per_solver_run():
         assert mdl.counters()["launches"] == expected
 
 
-@pytest.mark.parametrize("precision", [ca.PRECISION.BF16, ca.PRECISION.FP32])
-def test_auto_training_reaches_fp32_cholesky_rmse(precision):
-    """Full-size workload 2 (69,878 x 10,677, 10M ratings, f = 64), 10 iterations.  (Scaled-down
-    copies of it over-fit, test RMSE ~1.34, where 6-step CG itself lands 2e-3 from Cholesky.)"""
-    tr, te, info = workload2(scale=1.0)
+@pytest.mark.parametrize("config,precision", [(2, ca.PRECISION.BF16), (2, ca.PRECISION.FP32),
+                                              (5, ca.PRECISION.BF16)])
+def test_auto_training_reaches_fp32_cholesky_rmse(config, precision):
+    """Full-size workload 2 (69,878 x 10,677, 10M ratings, f = 64) and 5 (283,228 x 58,098, 24.3M
+    ratings, f = 128, whose items lighter than f take CG under the tuner's agreement bound), 10
+    iterations.  (Scaled-down copies over-fit, test RMSE ~1.34, where 6-step CG itself lands 2e-3
+    from Cholesky.)"""
+    tr, te, info = ca.synth_generate(config, scale=1.0)
     with model(tr, te, info, ca.SOLVE_TYPE.CHOLESKY, ca.PRECISION.FP32) as ref:
         ref.train()
         r_ref = ref.rsme_test()
