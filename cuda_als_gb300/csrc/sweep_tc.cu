@@ -263,7 +263,8 @@ als_status tc_prepare(als_handle *h, std::string *why) {
     default: e = t->f8 ? tcg::configure_128_e4m3(smem_max) : tcg::configure_128(smem_max); break;
     }
     if (e != cudaSuccess) {
-        *why = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+        *why = std::string("configuring the tcgen05 sweep kernels (shared-memory limit, register "
+                           "split): ") + cudaGetErrorString(e);
         return ALS_ERR_CUDA;
     }
     return ALS_OK;

@@ -74,15 +74,31 @@ __host__ __device__ constexpr int nepi_of(int solver, int fp) {
     return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(solver, fp)
                                                                    : nbuf_of(solver, fp) / 2;
 }
-// Gather warps: as many as the registers the solvers need allow.  A launch's registers are
-// shared out per four warps, so above 640 threads a thread keeps 80 and at 640 it keeps 96: the
-// tensor-core CG (about 60 a thread) takes six, the other solvers two (the quad-blocked CG and the
-// Cholesky factor need 96 and 84 at four groups).
+// Gather warps: one warp issues a tile::gather4 only every ~90 cycles, so the gathers want as
+// many warps as the registers allow.  A launch's registers are shared out per four warps, so
+// above 640 threads a thread keeps 80 and at 640 it keeps 96.  The tensor-core CG (about 60 a
+// thread) takes six gather warps; the Cholesky factor, LU and the four-group quad-blocked CG (84
+// to 96 a thread) two.  The three-group quad-blocked CG at FP = 128 splits the registers
+// (setmaxnreg): launched with six gather warps at 96 a thread, its solver warpgroups take 128 and
+// the two service warpgroups (producer, MMA issuer, gather warps) give theirs back down to
+// SERVICE_REGS, the sum being exactly what the launch holds (launch_regs_of x threads).  (The
+// same split for the four groups at FP = 64 and 112, 80 a thread at launch, made their light rows,
+// bound by the solves, 1-8% slower.)
+__host__ __device__ constexpr bool regsplit_of(int solver, int fp) {
+    return cg_quad_rows(solver, fp) && fp == 128;
+}
 __host__ __device__ constexpr int ngather_of(int solver, int fp) {
-    return solver == 3 ? 6 : 2;
+    return solver == 3 || regsplit_of(solver, fp) ? 6 : 2;
 }
 __host__ __device__ constexpr int nthreads_of(int solver, int fp) {
     return 128 * nepi_of(solver, fp) + 32 * (2 + ngather_of(solver, fp));
+}
+constexpr int SERVICE_REGS = 48;
+__host__ __device__ constexpr int solver_regs_of(int solver, int fp) { return fp == 128 ? 128 : 96; }
+__host__ __device__ constexpr int launch_regs_of(int solver, int fp) {
+    return (solver_regs_of(solver, fp) * 128 * nepi_of(solver, fp) +
+            SERVICE_REGS * 32 * (2 + ngather_of(solver, fp))) /
+           nthreads_of(solver, fp);
 }
 
 // Bound of every spin-wait: the role waits use Params::wait_ns (the handle's limit, by default
@@ -897,6 +913,19 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     // a Gram MMA and an N = 16 right-hand-side MMA (the same e4m3 products, summed in one pass).
     constexpr bool FUSED = SOLVER == SOLVER_CGTC && FP <= 112;
     static_assert(NGATHER <= MAX_NGATHER, "");
+    // Register split: setmaxnreg acts per warpgroup, so the solver warps and the service warps
+    // each form whole warpgroups, and the registers the solvers take are exactly those the
+    // service warps give back out of the launch's own (a larger .inc would wait forever; the host
+    // also checks the compiled count, configure_fp).
+    constexpr bool REGSPLIT = regsplit_of(SOLVER, FP);
+    static_assert(!REGSPLIT || (WP % 4 == 0 && (2 + NGATHER) % 4 == 0), "whole warpgroups");
+    static_assert(!REGSPLIT || (solver_regs_of(SOLVER, FP) * 128 * NEPI +
+                                    SERVICE_REGS * 32 * (2 + NGATHER) ==
+                                launch_regs_of(SOLVER, FP) * nthreads_of(SOLVER, FP)),
+                  "register split");
+    static_assert(!REGSPLIT || (launch_regs_of(SOLVER, FP) % 8 == 0 &&
+                                launch_regs_of(SOLVER, FP) * nthreads_of(SOLVER, FP) <= 65536),
+                  "register split");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *ring = smem;
@@ -970,241 +999,10 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
-    if (warp == WP) {
-        // ------------------------------------------------------------------ producer
-        // Two cursors walk the same sequence of stages (KC ratings of one row each).  The
-        // look-ahead cursor issues a stage's column ids and ratings as 4-byte cp.async into the
-        // metadata ring MD stages ahead, with its Meta; the publishing cursor waits for that
-        // cp.async group and publishes the stage to the gather warps, which do the rest.  Rows
-        // come in chunks from the atomic counter (one at a time among the first `head` slots, the
-        // heaviest rows, then CH at a time), pipelined two chunks ahead so the dependent
-        // order[] -> ptr[] loads have landed when a chunk starts.
-        constexpr int CH = 8;
-        const int head = 4 * (int)gridDim.x;
-        int grab_size = 1;
-        auto grab = [&](int &cb, int &cc) {
-            int b = 0;
-            if (lane == 0) b = atomicAdd(p.work, grab_size);
-            b = __shfl_sync(0xffffffffu, b, 0);
-            cb = b;
-            cc = max(0, min(grab_size, p.nrows - b));
-            if (b + grab_size >= head) grab_size = CH;
-        };
-        // chunk pipeline: current (row, beg, end in lane j), next (row, beg, end), next-next (row)
-        int ccnt, crow, cbeg, cend, n1cnt, n1row, n1beg, n1end, n2cnt, n2row;
-        {
-            int cb;
-            grab(cb, ccnt);
-            crow = lane < ccnt ? p.order[cb + lane] : 0;
-            grab(cb, n1cnt);
-            n1row = lane < n1cnt ? p.order[cb + lane] : 0;
-            grab(cb, n2cnt);
-            n2row = lane < n2cnt ? p.order[cb + lane] : 0;
-            cbeg = lane < ccnt ? p.ptr[crow] : 0;
-            cend = lane < ccnt ? p.ptr[crow + 1] : 0;
-            n1beg = lane < n1cnt ? p.ptr[n1row] : 0;
-            n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
-        }
-        const uint64_t stream_pol = l2_evict_first_policy();  // column ids and ratings: once
-        int aj = 0;                                          // look-ahead cursor: row of chunk
-        int abase = __shfl_sync(0xffffffffu, cbeg, 0);       // and first rating of its stage
-        uint32_t gen = 0;                                    // stages issued by the look-ahead
-        // the metadata slot of stage g is free once the gather warp of stage g - MR has taken the
-        // column ids, ratings and Meta out of it (bounded wait; false on timeout or abort)
-        auto slot_free = [&](uint32_t g) -> bool {
-            if (g < (uint32_t)MR) return true;
-            const uint32_t old = g - MR;
-            int r = 1;
-            if (lane == 0) {
-                const volatile int *d = done + old % NGATHER;
-                const unsigned long long t0 = now_ns();
-                for (uint32_t k = 0;; ++k) {
-                    if ((uint32_t)*d > old) break;
-                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
-                        r = 0;
-                        break;
-                    }
-                }
-                __threadfence_block();
-            }
-            return __shfl_sync(0xffffffffu, r, 0) != 0;
-        };
-        // issue the metadata of stage `gen`: 1 issued, 0 no rows left, -1 its slot never freed
-        auto generate = [&]() -> int {
-            while (aj >= ccnt) {
-                if (ccnt <= 0) return 0;
-                ccnt = n1cnt; crow = n1row; cbeg = n1beg; cend = n1end;
-                n1cnt = n2cnt; n1row = n2row;
-                n1beg = lane < n1cnt ? p.ptr[n1row] : 0;     // n2's row ids landed a chunk ago
-                n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
-                int cb;
-                grab(cb, n2cnt);
-                n2row = lane < n2cnt ? p.order[cb + lane] : 0;
-                aj = 0;
-                if (ccnt <= 0) return 0;
-                abase = __shfl_sync(0xffffffffu, cbeg, 0);
-            }
-            if (!slot_free(gen)) return -1;
-            const int row = __shfl_sync(0xffffffffu, crow, aj);
-            const int beg = __shfl_sync(0xffffffffu, cbeg, aj);
-            const int end = __shfl_sync(0xffffffffu, cend, aj);
-            const int cnt = min(KC, end - abase);
-            const int slot = (int)(gen % MR);
-            int32_t *mc = mcol + slot * KC;
-            float *mv = mval + slot * KC;
-#pragma unroll
-            for (int h = 0; h < KC; h += 32) {
-                if (lane + h < cnt) {
-                    cp_async4(smem_u32(mc + lane + h), p.idx + abase + lane + h, stream_pol);
-                    cp_async4(smem_u32(mv + lane + h), p.val + abase + lane + h, stream_pol);
-                } else {
-                    mc[lane + h] = p.zero_row;   // the ragged tail gathers the all-zero row
-                    mv[lane + h] = 0.f;
-                }
-            }
-            cp_commit();
-            if (lane == 0) {
-                Meta m;
-                m.row = row;
-                m.cnt = cnt;
-                m.flags = (abase == beg ? 1 : 0) | (abase + KC >= end ? 2 : 0);
-                m.nu = end - beg;
-                mmeta[slot] = m;
-            }
-            abase += KC;
-            if (abase >= end) {
-                ++aj;
-                abase = aj < ccnt ? __shfl_sync(0xffffffffu, cbeg, aj < ccnt ? aj : 0) : 0;
-            }
-            ++gen;
-            return 1;
-        };
-        bool ok = true;
-        int more = 1;
-        for (int k = 0; k < MD && more == 1; ++k) more = generate();
-        if (more < 0) ok = false;
-        uint32_t it = 0;  // stages published
-        while (ok && it < gen) {
-            // stage it's metadata group: at most gen - it - 1 younger groups may stay pending
-            if (gen - it - 1 >= (uint32_t)(MD - 1))
-                cp_wait<MD - 1>();
-            else
-                cp_wait<0>();
-            __syncwarp();  // every lane's copies (and tail fills) of the stage are in place
-            if (lane == 0) {
-                __threadfence_block();
-                *pub = (int)(it + 1);
-            }
-            __syncwarp();
-            ++it;
-            if (more == 1) {
-                more = generate();
-                if (more < 0) ok = false;
-            }
-        }
-        // nothing of this warp may be in flight when the CTA tears down
-        cp_wait<0>();
-        __syncwarp();
-        if (lane == 0) {  // *pub is now the number of stages; the gather warps add the end marker
-            __threadfence_block();
-            *fin = 1;
-        }
-        if (!ok) {
-            *abort = 1;
-            if (lane == 0) atomicAdd(&p.flags[2], 1);
-        }
-    } else if (warp == WM) {
-        // ------------------------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            const int ng_mma = FUSED ? p.ng + 16 : p.ng;
-            const uint32_t idesc_g = F8 ? idesc_e4m3(128, ng_mma, true, true)
-                                        : idesc_bf16(128, ng_mma, true, true);
-            const uint32_t idesc_r = F8 ? idesc_e4m3(128, 16, true, false)
-                                        : idesc_bf16(128, 16, true, false);
-            const uint32_t ring_s = smem_u32(ring);
-            uint32_t it = 0, acc_it = 0, buf = 0;
-            bool ok = true;
-            auto take_buffer = [&]() -> bool {  // wait until accumulator acc_it % nbuf is free
-                buf = acc_it % nbuf;
-                const uint32_t use = acc_it / nbuf;
-                if (use >= 1 &&
-                    !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort, p.wait_ns))
-                    return false;
-                tc_fence_after();
-                return true;
-            };
-            for (;;) {
-                const int s = it % NSTAGE;
-                // (every writer of the stage's operands fenced its generic stores into the async
-                // proxy before it arrived: the acquire of this wait is all the MMA needs)
-                if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort,
-                               p.wait_ns)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                const Meta m = smeta[s];
-                if (m.row < 0) {  // end of work: one end marker per solver warpgroup
-                    for (int g = 0; g < NEPI && ok; ++g) {
-                        if (!take_buffer()) { ok = false; break; }
-                        ameta[buf] = m;
-                        mbar_arrive(smem_u32(&acc_meta[buf]));
-                        ++acc_it;
-                    }
-                    break;
-                }
-                if ((m.flags & 1) && !take_buffer()) { ok = false; break; }
-                const uint32_t dg = tmem_base + buf * p.acc_stride;
-                const uint32_t db = dg + p.ng;
-                const uint32_t tile_s = ring_s + s * SBYTES;
-                if constexpr (F8) {
-                    // K = 32 ratings (four 8-rating groups, 4 KB of the one-atom panel) and the
-                    // matching 32 bytes of the rating tile's row per MMA
-                    const int nk = (m.cnt + F8_K - 1) / F8_K;
-                    for (int kk = 0; kk < nk; ++kk) {
-                        const uint64_t ad =
-                            sdesc(tile_s + kk * 4 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
-                        const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
-                        mma_e4m3(dg, ad, ad, idesc_g, accum);
-                        if (!FUSED) {
-                            const uint64_t rd = sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
-                            mma_e4m3(db, ad, rd, idesc_r, accum);
-                        }
-                    }
-                } else {
-                    const int nk = (m.cnt + 15) >> 4;
-                    for (int kk = 0; kk < nk; ++kk) {
-                        const uint64_t ad =
-                            sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
-                        const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
-                        mma_bf16(dg, ad, ad, idesc_g, accum);
-                        if (!FUSED) {
-                            const uint64_t rd =
-                                sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
-                            mma_bf16(db, ad, rd, idesc_r, accum);
-                        }
-                    }
-                }
-                mma_commit(smem_u32(&empty[s]));
-                if (m.flags & 2) {
-                    ameta[buf] = m;
-                    // committed for empty rows too, so buffer b's phase count is its use count
-                    mma_commit(smem_u32(&acc_full[buf]));
-                    mbar_arrive(smem_u32(&acc_meta[buf]));
-                    ++acc_it;
-                }
-                ++it;
-            }
-            // drain: every MMA issued so far has completed before TMEM is released
-            mma_commit(smem_u32(drain));
-            if (!mbar_wait(smem_u32(drain), 0, nullptr, WAIT_NS)) ok = false;
-            if (!ok) {
-                *abort = 1;
-                atomicAdd(&p.flags[2], 1);
-            }
-        }
-        __syncwarp();
-    } else if (warp < WP) {
+    // (the solver warpgroups first: each role's register budget covers the code it runs)
+    if (warp < WP) {
+        if constexpr (REGSPLIT)
+            asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(solver_regs_of(SOLVER, FP)) : "memory");
         // ------------------------------------------------------------------ solver warpgroups
         const int g = warp >> 2;
         const int et = tid - 128 * g;                // 0..127 inside the group
@@ -1259,179 +1057,417 @@ __global__ void __launch_bounds__(nthreads_of(SOLVER, FP), 1)
             if (SOLVER == SOLVER_CGTC ? lane == 0 : et == 0) atomicAdd(&p.flags[2], 1);
         }
     } else {
-        // ------------------------------------------------------------------ gather warps
-        // Warp h takes every NGATHER-th stage from t = h once the producer has published it:
-        // it waits for the stage's ring slot, writes the rating tile, reads the column ids and
-        // Meta out of the metadata slot (handing the slot back), arms the stage's full barrier
-        // with the byte count and issues one tile::gather4 per lane (4 ratings x 64 features).
-        // The warp whose turn comes after the last stage writes the end marker (row = -1).
-        const int h = warp - WG;
-        const int natoms = F8 ? 1 : (p.fst > 64 ? 2 : 1);
-        const int gq = lane & 15, ga = lane >> 4;  // this lane's 4-rating quad, atom
-        const uint64_t keep = l2_evict_last_policy();
-        bool ok = true;
-        for (uint32_t t = (uint32_t)h;; t += NGATHER) {
-            int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out or aborted
-            uint32_t total = 0;
-            if (lane == 0) {
-                const unsigned long long t0 = now_ns();
-                for (uint32_t k = 0;; ++k) {
-                    if ((uint32_t)*pub > t) { go = 1; break; }
-                    if (*fin) {
-                        total = (uint32_t)*pub;
-                        go = total > t ? 1 : 0;
-                        break;
-                    }
-                    if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
-                        go = -1;
-                        break;
-                    }
-                }
-                __threadfence_block();
+        if constexpr (REGSPLIT)
+            asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(SERVICE_REGS) : "memory");
+        if (warp == WP) {
+            // ------------------------------------------------------------------ producer
+            // Two cursors walk the same sequence of stages (KC ratings of one row each).  The
+            // look-ahead cursor issues a stage's column ids and ratings as 4-byte cp.async into the
+            // metadata ring MD stages ahead, with its Meta; the publishing cursor waits for that
+            // cp.async group and publishes the stage to the gather warps, which do the rest.  Rows
+            // come in chunks from the atomic counter (one at a time among the first `head` slots, the
+            // heaviest rows, then CH at a time), pipelined two chunks ahead so the dependent
+            // order[] -> ptr[] loads have landed when a chunk starts.
+            constexpr int CH = 8;
+            const int head = 4 * (int)gridDim.x;
+            int grab_size = 1;
+            auto grab = [&](int &cb, int &cc) {
+                int b = 0;
+                if (lane == 0) b = atomicAdd(p.work, grab_size);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                cb = b;
+                cc = max(0, min(grab_size, p.nrows - b));
+                if (b + grab_size >= head) grab_size = CH;
+            };
+            // chunk pipeline: current (row, beg, end in lane j), next (row, beg, end), next-next (row)
+            int ccnt, crow, cbeg, cend, n1cnt, n1row, n1beg, n1end, n2cnt, n2row;
+            {
+                int cb;
+                grab(cb, ccnt);
+                crow = lane < ccnt ? p.order[cb + lane] : 0;
+                grab(cb, n1cnt);
+                n1row = lane < n1cnt ? p.order[cb + lane] : 0;
+                grab(cb, n2cnt);
+                n2row = lane < n2cnt ? p.order[cb + lane] : 0;
+                cbeg = lane < ccnt ? p.ptr[crow] : 0;
+                cend = lane < ccnt ? p.ptr[crow + 1] : 0;
+                n1beg = lane < n1cnt ? p.ptr[n1row] : 0;
+                n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
             }
-            go = __shfl_sync(0xffffffffu, go, 0);
-            total = __shfl_sync(0xffffffffu, total, 0);
-            __syncwarp();  // the lanes' reads of the stage's metadata follow lane 0's acquire
-            if (go < 0) {
-                ok = false;
-                break;
-            }
-            if (go == 0 && t != total) break;  // another warp writes the end marker
-            const int s = t % NSTAGE;
-            if (t >= NSTAGE) {
-                // the slot's previous stage (another warp's) is armed first: then the slot's
-                // empty barrier is at most one phase behind the one waited for below, so its
-                // parity cannot match an older phase
-                int armed_ok = 1;
+            const uint64_t stream_pol = l2_evict_first_policy();  // column ids and ratings: once
+            int aj = 0;                                          // look-ahead cursor: row of chunk
+            int abase = __shfl_sync(0xffffffffu, cbeg, 0);       // and first rating of its stage
+            uint32_t gen = 0;                                    // stages issued by the look-ahead
+            // the metadata slot of stage g is free once the gather warp of stage g - MR has taken the
+            // column ids, ratings and Meta out of it (bounded wait; false on timeout or abort)
+            auto slot_free = [&](uint32_t g) -> bool {
+                if (g < (uint32_t)MR) return true;
+                const uint32_t old = g - MR;
+                int r = 1;
                 if (lane == 0) {
+                    const volatile int *d = done + old % NGATHER;
                     const unsigned long long t0 = now_ns();
                     for (uint32_t k = 0;; ++k) {
-                        if (armed[s] >= (int)(t - NSTAGE)) break;
+                        if ((uint32_t)*d > old) break;
                         if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
-                            armed_ok = 0;
+                            r = 0;
                             break;
                         }
                     }
                     __threadfence_block();
                 }
-                if (!__shfl_sync(0xffffffffu, armed_ok, 0)) {
-                    ok = false;
-                    break;
+                return __shfl_sync(0xffffffffu, r, 0) != 0;
+            };
+            // issue the metadata of stage `gen`: 1 issued, 0 no rows left, -1 its slot never freed
+            auto generate = [&]() -> int {
+                while (aj >= ccnt) {
+                    if (ccnt <= 0) return 0;
+                    ccnt = n1cnt; crow = n1row; cbeg = n1beg; cend = n1end;
+                    n1cnt = n2cnt; n1row = n2row;
+                    n1beg = lane < n1cnt ? p.ptr[n1row] : 0;     // n2's row ids landed a chunk ago
+                    n1end = lane < n1cnt ? p.ptr[n1row + 1] : 0;
+                    int cb;
+                    grab(cb, n2cnt);
+                    n2row = lane < n2cnt ? p.order[cb + lane] : 0;
+                    aj = 0;
+                    if (ccnt <= 0) return 0;
+                    abase = __shfl_sync(0xffffffffu, cbeg, 0);
                 }
-            }
-            if (t >= NSTAGE &&
-                !mbar_wait_warp(smem_u32(&empty[s]), ((t / NSTAGE) - 1) & 1, abort, p.wait_ns)) {
-                ok = false;
-                break;
-            }
-            if (go == 0) {  // t == total: the end marker, one stage with row = -1
+                if (!slot_free(gen)) return -1;
+                const int row = __shfl_sync(0xffffffffu, crow, aj);
+                const int beg = __shfl_sync(0xffffffffu, cbeg, aj);
+                const int end = __shfl_sync(0xffffffffu, cend, aj);
+                const int cnt = min(KC, end - abase);
+                const int slot = (int)(gen % MR);
+                int32_t *mc = mcol + slot * KC;
+                float *mv = mval + slot * KC;
+    #pragma unroll
+                for (int h = 0; h < KC; h += 32) {
+                    if (lane + h < cnt) {
+                        cp_async4(smem_u32(mc + lane + h), p.idx + abase + lane + h, stream_pol);
+                        cp_async4(smem_u32(mv + lane + h), p.val + abase + lane + h, stream_pol);
+                    } else {
+                        mc[lane + h] = p.zero_row;   // the ragged tail gathers the all-zero row
+                        mv[lane + h] = 0.f;
+                    }
+                }
+                cp_commit();
                 if (lane == 0) {
                     Meta m;
-                    m.row = -1;
-                    m.cnt = 0;
-                    m.flags = 3;
-                    m.nu = 0;
-                    smeta[s] = m;
-                    armed[s] = (int)t;  // (its phase completes on this arrive: no bytes)
-                    mbar_arrive(smem_u32(&full[s]));
-                    if (FUSED) mbar_arrive(smem_u32(&ready[s]));
+                    m.row = row;
+                    m.cnt = cnt;
+                    m.flags = (abase == beg ? 1 : 0) | (abase + KC >= end ? 2 : 0);
+                    m.nu = end - beg;
+                    mmeta[slot] = m;
+                }
+                abase += KC;
+                if (abase >= end) {
+                    ++aj;
+                    abase = aj < ccnt ? __shfl_sync(0xffffffffu, cbeg, aj < ccnt ? aj : 0) : 0;
+                }
+                ++gen;
+                return 1;
+            };
+            bool ok = true;
+            int more = 1;
+            for (int k = 0; k < MD && more == 1; ++k) more = generate();
+            if (more < 0) ok = false;
+            uint32_t it = 0;  // stages published
+            while (ok && it < gen) {
+                // stage it's metadata group: at most gen - it - 1 younger groups may stay pending
+                if (gen - it - 1 >= (uint32_t)(MD - 1))
+                    cp_wait<MD - 1>();
+                else
+                    cp_wait<0>();
+                __syncwarp();  // every lane's copies (and tail fills) of the stage are in place
+                if (lane == 0) {
+                    __threadfence_block();
+                    *pub = (int)(it + 1);
                 }
                 __syncwarp();
-                break;
+                ++it;
+                if (more == 1) {
+                    more = generate();
+                    if (more < 0) ok = false;
+                }
             }
-            const int slot = (int)(t % MR);
-            Meta m;  // read by lane 0 (which saw the stage published), handed to the warp
-            {
-                int4 w = make_int4(0, 0, 0, 0);
-                if (lane == 0) w = *reinterpret_cast<const int4 *>(&mmeta[slot]);
-                m.row = __shfl_sync(0xffffffffu, w.x, 0);
-                m.cnt = __shfl_sync(0xffffffffu, w.y, 0);
-                m.flags = __shfl_sync(0xffffffffu, w.z, 0);
-                m.nu = __shfl_sync(0xffffffffu, w.w, 0);
-            }
-            uint8_t *tile = ring + s * SBYTES;
-            __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TBYTES);
-            if constexpr (F8) {  // e4m3 ratings (star ratings are exact), bytes 0..63 of row 0
-                uint8_t *rt8 = tile + TBYTES;
-                rt8[lane] = __nv_cvt_float_to_fp8(mval[slot * KC + lane], __NV_SATFINITE, __NV_E4M3);
-                rt8[lane + 32] =
-                    __nv_cvt_float_to_fp8(mval[slot * KC + lane + 32], __NV_SATFINITE, __NV_E4M3);
-            } else {
-                rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
-                rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
-            }
-            // the MMA reads ratings [0, 16 nk) (FP8: [0, 32 nk)): gather their quads (the ragged
-            // tail's column ids point at the zero row), 512 bytes per quad and atom
-            const int nq = F8 ? ((m.cnt + F8_K - 1) / F8_K) * (F8_K / 4) : ((m.cnt + 15) >> 4) * 4;
-            const bool mine = gq < nq && ga < natoms;
-            int32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-            if (mine) {
-                const int32_t *q = mcol + slot * KC + 4 * gq;
-                r0 = q[0];
-                r1 = q[1];
-                r2 = q[2];
-                r3 = q[3];
-            }
-            // the rating tile is a generic store: visible to the tensor core (async proxy)
-            // before the stage can complete
-            fence_async_smem();
-            __syncwarp();  // every lane has read the metadata slot and written its ratings
-            if (lane == 0) {
+            // nothing of this warp may be in flight when the CTA tears down
+            cp_wait<0>();
+            __syncwarp();
+            if (lane == 0) {  // *pub is now the number of stages; the gather warps add the end marker
                 __threadfence_block();
-                done[h] = (int)(t + 1);  // the metadata slot may be refilled
-                smeta[s] = m;
-                armed[s] = (int)t;
-                mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
+                *fin = 1;
+            }
+            if (!ok) {
+                *abort = 1;
+                if (lane == 0) atomicAdd(&p.flags[2], 1);
+            }
+        } else if (warp == WM) {
+            // ------------------------------------------------------------------ MMA issuer
+            if (lane == 0) {
+                const int ng_mma = FUSED ? p.ng + 16 : p.ng;
+                const uint32_t idesc_g = F8 ? idesc_e4m3(128, ng_mma, true, true)
+                                            : idesc_bf16(128, ng_mma, true, true);
+                const uint32_t idesc_r = F8 ? idesc_e4m3(128, 16, true, false)
+                                            : idesc_bf16(128, 16, true, false);
+                const uint32_t ring_s = smem_u32(ring);
+                uint32_t it = 0, acc_it = 0, buf = 0;
+                bool ok = true;
+                auto take_buffer = [&]() -> bool {  // wait until accumulator acc_it % nbuf is free
+                    buf = acc_it % nbuf;
+                    const uint32_t use = acc_it / nbuf;
+                    if (use >= 1 &&
+                        !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1, abort, p.wait_ns))
+                        return false;
+                    tc_fence_after();
+                    return true;
+                };
+                for (;;) {
+                    const int s = it % NSTAGE;
+                    // (every writer of the stage's operands fenced its generic stores into the async
+                    // proxy before it arrived: the acquire of this wait is all the MMA needs)
+                    if (!mbar_wait(smem_u32(FUSED ? &ready[s] : &full[s]), (it / NSTAGE) & 1, abort,
+                                   p.wait_ns)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const Meta m = smeta[s];
+                    if (m.row < 0) {  // end of work: one end marker per solver warpgroup
+                        for (int g = 0; g < NEPI && ok; ++g) {
+                            if (!take_buffer()) { ok = false; break; }
+                            ameta[buf] = m;
+                            mbar_arrive(smem_u32(&acc_meta[buf]));
+                            ++acc_it;
+                        }
+                        break;
+                    }
+                    if ((m.flags & 1) && !take_buffer()) { ok = false; break; }
+                    const uint32_t dg = tmem_base + buf * p.acc_stride;
+                    const uint32_t db = dg + p.ng;
+                    const uint32_t tile_s = ring_s + s * SBYTES;
+                    if constexpr (F8) {
+                        // K = 32 ratings (four 8-rating groups, 4 KB of the one-atom panel) and the
+                        // matching 32 bytes of the rating tile's row per MMA
+                        const int nk = (m.cnt + F8_K - 1) / F8_K;
+                        for (int kk = 0; kk < nk; ++kk) {
+                            const uint64_t ad =
+                                sdesc(tile_s + kk * 4 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
+                            const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
+                            mma_e4m3(dg, ad, ad, idesc_g, accum);
+                            if (!FUSED) {
+                                const uint64_t rd = sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
+                                mma_e4m3(db, ad, rd, idesc_r, accum);
+                            }
+                        }
+                    } else {
+                        const int nk = (m.cnt + 15) >> 4;
+                        for (int kk = 0; kk < nk; ++kk) {
+                            const uint64_t ad =
+                                sdesc(tile_s + kk * 2 * ATOM_BYTES, ATOM_STRIDE, ATOM_BYTES);
+                            const uint32_t accum = ((m.flags & 1) && kk == 0) ? 0u : 1u;
+                            mma_bf16(dg, ad, ad, idesc_g, accum);
+                            if (!FUSED) {
+                                const uint64_t rd =
+                                    sdesc(tile_s + TBYTES + kk * 32, 16, ATOM_BYTES);
+                                mma_bf16(db, ad, rd, idesc_r, accum);
+                            }
+                        }
+                    }
+                    mma_commit(smem_u32(&empty[s]));
+                    if (m.flags & 2) {
+                        ameta[buf] = m;
+                        // committed for empty rows too, so buffer b's phase count is its use count
+                        mma_commit(smem_u32(&acc_full[buf]));
+                        mbar_arrive(smem_u32(&acc_meta[buf]));
+                        ++acc_it;
+                    }
+                    ++it;
+                }
+                // drain: every MMA issued so far has completed before TMEM is released
+                mma_commit(smem_u32(drain));
+                if (!mbar_wait(smem_u32(drain), 0, nullptr, WAIT_NS)) ok = false;
+                if (!ok) {
+                    *abort = 1;
+                    atomicAdd(&p.flags[2], 1);
+                }
             }
             __syncwarp();
-            if (mine) {
-                const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE + (gq >> 1) * ATOM_BYTES +
-                                     (gq & 1) * 512;
-                tma_gather4(dst, &p.tmap, 64 * ga, r0, r1, r2, r3, smem_u32(&full[s]), keep);
-            }
-            __syncwarp();
-            if constexpr (FUSED) {
-                // the stage's ratings into feature column ng, once its gathered rows have landed
-                if (!mbar_wait_warp(smem_u32(&full[s]), (t / NSTAGE) & 1, abort, p.wait_ns)) {
+        } else {
+            // ------------------------------------------------------------------ gather warps
+            // Warp h takes every NGATHER-th stage from t = h once the producer has published it:
+            // it waits for the stage's ring slot, writes the rating tile, reads the column ids and
+            // Meta out of the metadata slot (handing the slot back), arms the stage's full barrier
+            // with the byte count and issues one tile::gather4 per lane (4 ratings x 64 features).
+            // The warp whose turn comes after the last stage writes the end marker (row = -1).
+            const int h = warp - WG;
+            const int natoms = F8 ? 1 : (p.fst > 64 ? 2 : 1);
+            const int gq = lane & 15, ga = lane >> 4;  // this lane's 4-rating quad, atom
+            const uint64_t keep = l2_evict_last_policy();
+            bool ok = true;
+            for (uint32_t t = (uint32_t)h;; t += NGATHER) {
+                int go = 0;  // 1: stage t is published, 0: no more stages, -1: timed out or aborted
+                uint32_t total = 0;
+                if (lane == 0) {
+                    const unsigned long long t0 = now_ns();
+                    for (uint32_t k = 0;; ++k) {
+                        if ((uint32_t)*pub > t) { go = 1; break; }
+                        if (*fin) {
+                            total = (uint32_t)*pub;
+                            go = total > t ? 1 : 0;
+                            break;
+                        }
+                        if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
+                            go = -1;
+                            break;
+                        }
+                    }
+                    __threadfence_block();
+                }
+                go = __shfl_sync(0xffffffffu, go, 0);
+                total = __shfl_sync(0xffffffffu, total, 0);
+                __syncwarp();  // the lanes' reads of the stage's metadata follow lane 0's acquire
+                if (go < 0) {
                     ok = false;
                     break;
                 }
-                if constexpr (F8) {
-                    // one 128-feature atom of bytes: column ng (a multiple of 16) starts
-                    // 16-byte chunk ng / 16 of each row, before the 128-byte swizzle
-                    const int rc = p.ng >> 4;
-                    const uint8_t *rt8 = tile + TBYTES;
-                    for (int k = lane; k < 4 * nq; k += 32)
-                        tile[(k >> 3) * ATOM_BYTES + (k & 7) * 128 + ((rc ^ (k & 7)) << 4)] =
-                            rt8[k];
-                } else {
-                    const int ra = p.ng >> 6, rc = (p.ng & 63) >> 3;  // column ng: atom, chunk
-                    for (int k = lane; k < 4 * nq; k += 32)
-                        *reinterpret_cast<__nv_bfloat16 *>(tile + ra * ATOM_STRIDE +
-                                                           (k >> 3) * ATOM_BYTES + (k & 7) * 128 +
-                                                           ((rc ^ (k & 7)) << 4)) = rt[k];
+                if (go == 0 && t != total) break;  // another warp writes the end marker
+                const int s = t % NSTAGE;
+                if (t >= NSTAGE) {
+                    // the slot's previous stage (another warp's) is armed first: then the slot's
+                    // empty barrier is at most one phase behind the one waited for below, so its
+                    // parity cannot match an older phase
+                    int armed_ok = 1;
+                    if (lane == 0) {
+                        const unsigned long long t0 = now_ns();
+                        for (uint32_t k = 0;; ++k) {
+                            if (armed[s] >= (int)(t - NSTAGE)) break;
+                            if ((k & 255) == 255 && (*abort || now_ns() - t0 > p.wait_ns)) {
+                                armed_ok = 0;
+                                break;
+                            }
+                            }
+                        __threadfence_block();
+                    }
+                    if (!__shfl_sync(0xffffffffu, armed_ok, 0)) {
+                        ok = false;
+                        break;
+                    }
                 }
-                fence_async_smem();  // generic stores, read by the tensor core
+                if (t >= NSTAGE &&
+                    !mbar_wait_warp(smem_u32(&empty[s]), ((t / NSTAGE) - 1) & 1, abort, p.wait_ns)) {
+                    ok = false;
+                    break;
+                }
+                if (go == 0) {  // t == total: the end marker, one stage with row = -1
+                    if (lane == 0) {
+                        Meta m;
+                        m.row = -1;
+                        m.cnt = 0;
+                        m.flags = 3;
+                        m.nu = 0;
+                        smeta[s] = m;
+                        armed[s] = (int)t;  // (its phase completes on this arrive: no bytes)
+                        mbar_arrive(smem_u32(&full[s]));
+                        if (FUSED) mbar_arrive(smem_u32(&ready[s]));
+                    }
+                    __syncwarp();
+                    break;
+                }
+                const int slot = (int)(t % MR);
+                Meta m;  // read by lane 0 (which saw the stage published), handed to the warp
+                {
+                    int4 w = make_int4(0, 0, 0, 0);
+                    if (lane == 0) w = *reinterpret_cast<const int4 *>(&mmeta[slot]);
+                    m.row = __shfl_sync(0xffffffffu, w.x, 0);
+                    m.cnt = __shfl_sync(0xffffffffu, w.y, 0);
+                    m.flags = __shfl_sync(0xffffffffu, w.z, 0);
+                    m.nu = __shfl_sync(0xffffffffu, w.w, 0);
+                }
+                uint8_t *tile = ring + s * SBYTES;
+                __nv_bfloat16 *rt = reinterpret_cast<__nv_bfloat16 *>(tile + TBYTES);
+                if constexpr (F8) {  // e4m3 ratings (star ratings are exact), bytes 0..63 of row 0
+                    uint8_t *rt8 = tile + TBYTES;
+                    rt8[lane] = __nv_cvt_float_to_fp8(mval[slot * KC + lane], __NV_SATFINITE, __NV_E4M3);
+                    rt8[lane + 32] =
+                        __nv_cvt_float_to_fp8(mval[slot * KC + lane + 32], __NV_SATFINITE, __NV_E4M3);
+                } else {
+                    rt[lane] = __float2bfloat16_rn(mval[slot * KC + lane]);
+                    rt[lane + 32] = __float2bfloat16_rn(mval[slot * KC + lane + 32]);
+                }
+                // the MMA reads ratings [0, 16 nk) (FP8: [0, 32 nk)): gather their quads (the ragged
+                // tail's column ids point at the zero row), 512 bytes per quad and atom
+                const int nq = F8 ? ((m.cnt + F8_K - 1) / F8_K) * (F8_K / 4) : ((m.cnt + 15) >> 4) * 4;
+                const bool mine = gq < nq && ga < natoms;
+                int32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+                if (mine) {
+                    const int32_t *q = mcol + slot * KC + 4 * gq;
+                    r0 = q[0];
+                    r1 = q[1];
+                    r2 = q[2];
+                    r3 = q[3];
+                }
+                // the rating tile is a generic store: visible to the tensor core (async proxy)
+                // before the stage can complete
+                fence_async_smem();
+                __syncwarp();  // every lane has read the metadata slot and written its ratings
+                if (lane == 0) {
+                    __threadfence_block();
+                    done[h] = (int)(t + 1);  // the metadata slot may be refilled
+                    smeta[s] = m;
+                    armed[s] = (int)t;
+                    mbar_arrive_expect_tx(smem_u32(&full[s]), (uint32_t)(nq * natoms * 512));
+                }
                 __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&ready[s]));
+                if (mine) {
+                    const uint32_t dst = smem_u32(tile) + ga * ATOM_STRIDE + (gq >> 1) * ATOM_BYTES +
+                                         (gq & 1) * 512;
+                    tma_gather4(dst, &p.tmap, 64 * ga, r0, r1, r2, r3, smem_u32(&full[s]), keep);
+                }
+                __syncwarp();
+                if constexpr (FUSED) {
+                    // the stage's ratings into feature column ng, once its gathered rows have landed
+                    if (!mbar_wait_warp(smem_u32(&full[s]), (t / NSTAGE) & 1, abort, p.wait_ns)) {
+                        ok = false;
+                        break;
+                    }
+                    if constexpr (F8) {
+                        // one 128-feature atom of bytes: column ng (a multiple of 16) starts
+                        // 16-byte chunk ng / 16 of each row, before the 128-byte swizzle
+                        const int rc = p.ng >> 4;
+                        const uint8_t *rt8 = tile + TBYTES;
+                        for (int k = lane; k < 4 * nq; k += 32)
+                            tile[(k >> 3) * ATOM_BYTES + (k & 7) * 128 + ((rc ^ (k & 7)) << 4)] =
+                                rt8[k];
+                    } else {
+                        const int ra = p.ng >> 6, rc = (p.ng & 63) >> 3;  // column ng: atom, chunk
+                        for (int k = lane; k < 4 * nq; k += 32)
+                            *reinterpret_cast<__nv_bfloat16 *>(tile + ra * ATOM_STRIDE +
+                                                               (k >> 3) * ATOM_BYTES + (k & 7) * 128 +
+                                                               ((rc ^ (k & 7)) << 4)) = rt[k];
+                    }
+                    fence_async_smem();  // generic stores, read by the tensor core
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(&ready[s]));
+                }
             }
-        }
-        if (!ok) {
-            *abort = 1;
-            if (lane == 0) atomicAdd(&p.flags[2], 1);
-        }
-        // no gather may be in flight when the CTA tears down: once every gather warp is done,
-        // wait for the last stage armed in each ring slot (a slot is re-armed only after the
-        // MMA consumed its previous stage, so only the last can still be landing; bounded)
-        asm volatile("bar.sync %0, %1;" ::"r"(15), "r"(32 * NGATHER) : "memory");
-        if (h == 0 && lane == 0) {
-            for (int u = 0; u < NSTAGE; ++u) {
-                const int a = armed[u];
-                if (a >= 0)
-                    mbar_wait(smem_u32(&full[u]), (uint32_t)(a / NSTAGE) & 1, nullptr, WAIT_NS);
+            if (!ok) {
+                *abort = 1;
+                if (lane == 0) atomicAdd(&p.flags[2], 1);
             }
+            // no gather may be in flight when the CTA tears down: once every gather warp is done,
+            // wait for the last stage armed in each ring slot (a slot is re-armed only after the
+            // MMA consumed its previous stage, so only the last can still be landing; bounded)
+            asm volatile("bar.sync %0, %1;" ::"r"(15), "r"(32 * NGATHER) : "memory");
+            if (h == 0 && lane == 0) {
+                for (int u = 0; u < NSTAGE; ++u) {
+                    const int a = armed[u];
+                    if (a >= 0)
+                        mbar_wait(smem_u32(&full[u]), (uint32_t)(a / NSTAGE) & 1, nullptr, WAIT_NS);
+                }
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
 
     tc_fence_before();
@@ -1458,6 +1494,14 @@ cudaError_t configure_fp(size_t smem) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if ((size_t)maxsm < smem) return cudaErrorInvalidValue;
+    if (regsplit_of(SOLVER_CG, FP)) {
+        // the split's setmaxnreg.inc waits for registers the launch must hold: refuse a build
+        // whose compiled register count differs from the one the split was sized for
+        cudaFuncAttributes fa;
+        cudaError_t ea = cudaFuncGetAttributes(&fa, sweep_tc_kernel<FP, SOLVER_CG, F8>);
+        if (ea != cudaSuccess) return ea;
+        if (fa.numRegs != launch_regs_of(SOLVER_CG, FP)) return cudaErrorInvalidKernelImage;
+    }
     cudaError_t e = cudaFuncSetAttribute(sweep_tc_kernel<FP, SOLVER_CG, F8>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
     if (e == cudaSuccess)

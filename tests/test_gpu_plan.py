@@ -82,11 +82,12 @@ def test_fixed_solver_is_one_bucket():
             assert all(t["ms_cg"] < 0 for t in mdl.tuning(side))
 
 
-def test_auto_plan_launches_one_kernel_per_solver_run():
+@pytest.mark.parametrize("config,scale", [(2, 0.1), (3, 0.05)])
+def test_auto_plan_launches_one_kernel_per_solver_run(config, scale):
     """Adjacent buckets that settled on the same solver are contiguous rows of the order and share
     one launch: an epoch's kernel count is one BF16 quantise per side plus one launch per run of
-    equal solvers in each side's plan."""
-    tr, te, info = workload2()
+    equal solvers in each side's plan (f = 64 and f = 100)."""
+    tr, te, info = ca.synth_generate(config, scale=scale)
     with model(tr, te, info, ca.SOLVE_TYPE.AUTO, ca.PRECISION.BF16, iters=3) as mdl:
         mdl.init_factors()
         mdl.iterate(3)  # the tuning sweeps are over: the plan is final
