@@ -238,18 +238,21 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar)
                  : "memory");
 }
+// A try suspends the thread until the phase completes (the hardware wakes it then) or
+// MBAR_SUSPEND_NS pass, so a waiting warp takes no issue slots from the warps that work.
+constexpr uint32_t MBAR_SUSPEND_NS = 20000;
 __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(MBAR_SUSPEND_NS)
         : "memory");
     return ok != 0;
 }
-// Bounded wait (`limit` ns, checked every 16 failed tries); false on timeout or (when
-// abort != nullptr) once another role aborted.
+// Bounded wait (`limit` ns, checked every 16 failed tries, i.e. within ~0.3 ms); false on
+// timeout or (when abort != nullptr) once another role aborted.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort,
                                           unsigned long long limit) {
     if (mbar_try(bar, parity)) return true;
