@@ -74,8 +74,9 @@ __host__ __device__ constexpr int nepi_of(int solver, int fp) {
     return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(solver, fp)
                                                                    : nbuf_of(solver, fp) / 2;
 }
-// Gather warps: one warp issues a tile::gather4 only every ~90 cycles, so the gathers want as
-// many warps as the registers allow.  A launch's registers are shared out per four warps, so
+// Gather warps: one warp issues a tile::gather4 only every ~90 cycles, so the gathers want
+// several warps, up to about six (ten made the tensor-core CG slower: the SM's gathers are then
+// saturated and the extra warps only add hand-offs).  A launch's registers are shared out per four warps, so
 // above 640 threads a thread keeps 80 and at 640 it keeps 96.  The tensor-core CG (about 60 a
 // thread) takes six gather warps; the Cholesky factor, LU and the four-group quad-blocked CG (84
 // to 96 a thread) two.  The three-group quad-blocked CG at FP = 128 splits the registers
