@@ -74,16 +74,16 @@ __host__ __device__ constexpr int nepi_of(int solver, int fp) {
     return solver == 1 || solver == 3 || cg_quad_rows(solver, fp) ? nbuf_of(solver, fp)
                                                                    : nbuf_of(solver, fp) / 2;
 }
-// Gather warps: one warp issues a tile::gather4 only every ~90 cycles, so the gathers want
-// several warps, up to about six (ten made the tensor-core CG slower: the SM's gathers are then
-// saturated and the extra warps only add hand-offs).  A launch's registers are shared out per four warps, so
+// Gather warps: one warp issues a tile::gather4 only every ~90 cycles, so the gathers want several
+// warps, up to about six (ten made the tensor-core CG slower: the SM's gathers are then saturated
+// and the extra warps only add hand-offs).  A launch's registers are shared out per four warps, so
 // above 640 threads a thread keeps 80 and at 640 it keeps 96.  The tensor-core CG (about 60 a
 // thread) takes six gather warps; the Cholesky factor, LU and the four-group quad-blocked CG (84
 // to 96 a thread) two.  The three-group quad-blocked CG at FP = 128 splits the registers
 // (setmaxnreg): launched with six gather warps at 96 a thread, its solver warpgroups take 128 and
 // the two service warpgroups (producer, MMA issuer, gather warps) give theirs back down to
-// SERVICE_REGS, the sum being exactly what the launch holds (launch_regs_of x threads).  (The
-// same split for the four groups at FP = 64 and 112, 80 a thread at launch, made their light rows,
+// SERVICE_REGS, the sum being exactly what the launch holds (launch_regs_of x threads).  (The same
+// split for the four groups at FP = 64 and 112, 80 a thread at launch, made their light rows,
 // bound by the solves, 1-8% slower.)
 __host__ __device__ constexpr bool regsplit_of(int solver, int fp) {
     return cg_quad_rows(solver, fp) && fp == 128;
